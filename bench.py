@@ -1,0 +1,346 @@
+"""Benchmark: particle-steps/s of the SPH step on the 1,048,576-particle dam
+break (FP32), through the engine's C ABI, plus the batched and served forms.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload dam_break_1m|dam_break_16k|pool_drop_8m|batched|served]
+
+One JSON line on stdout (rank 0).  A "step" is one SPH step of the whole
+scene: density, force/integrate, scan, scatter, gather.  The device-resident
+value is timed with CUDA events on the engine's stream, one step at a time,
+with L2 flushed (256 MiB write) before each timed step; e2e repeats the step
+through the C ABI with the particle state copied in from pinned host memory
+and read back each step.  With --gpus N (torchrun) every rank advances its own
+replica of the scene (the path does not shard); value = all ranks' particle-
+steps / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+HBM_FALLBACK_GBS = 6800.0
+STAGES = ["density", "force", "scan", "scatter", "gather"]
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", HBM_FALLBACK_GBS)), "measured"
+    return HBM_FALLBACK_GBS, "fallback"
+
+
+def workload_scene(name: str, steps: int):
+    from sphfluidsimulation_gb300 import scenes
+    if name == "dam_break_1m":
+        return scenes.config1(steps)
+    if name == "dam_break_16k":
+        return scenes.config0(steps)
+    if name == "pool_drop_8m":
+        return scenes.config2(steps)
+    raise ValueError(name)
+
+
+def alg_bytes(stage: str, n: int, s: int) -> float:
+    """Algorithmic bytes per launch: each array read or written once in the
+    reference data flow with 2n buckets (per particle: density 28 B, force
+    68 B, scan 16 B, scatter 16 B, gather counted as the scatter's move 16 B;
+    static particles 20 B each per neighbour pass)."""
+    per = {"density": 28.0, "force": 68.0, "scan": 16.0, "scatter": 16.0, "gather": 16.0}[stage]
+    extra = 20.0 * s if stage in ("density", "force") else 0.0
+    return per * n + extra
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active," \
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown," \
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, value: float, local: int) -> float:
+    if pg is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=f"cuda:{local}")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (the oracle port of the reference CPU engine, threaded)
+# ---------------------------------------------------------------------------
+
+def cpu_baseline(scene, steps: int, warmup: int, threads: int):
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_lib import Oracle
+    o = Oracle(threads)
+    o.init(scene)
+    if warmup:
+        o.update(scene.dt, warmup)
+    t0 = time.perf_counter()
+    o.update(scene.dt, steps)
+    dt = time.perf_counter() - t0
+    return scene.n * steps / dt, dt
+
+
+def run_reference(args):
+    world, rank, local, pg = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0, None
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    scene = workload_scene(args.workload if args.workload not in ("batched", "served") else "dam_break_1m", 1)
+    # bounded sample: the steps of this run, capped so the run stays within minutes
+    per_step_s = scene.n / 3.0e6
+    steps = max(1, min(args.steps, int(60.0 / max(per_step_s, 1e-3))))
+    warm = min(args.warmup, 1)
+    value, secs = cpu_baseline(scene, steps, warm, threads)
+    sample = f"{scene.name}: {scene.n} particles, {steps} timed steps after {warm} warm-up, one Update() call"
+    line = {
+        "impl": "reference", "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
+        "n_gpus": world, "steps": steps, "warmup": warm, "ms_per_step": 1000.0 * secs / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded SplitMix64 dam break)",
+        "config": {"workload": scene.name, "particles": scene.n, "static_particles": scene.s,
+                   "h": scene.params.h, "dt": scene.dt},
+        "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm: the plain engine
+# ---------------------------------------------------------------------------
+
+def run_plain(args, world, rank, local, pg):
+    import torch
+    from sphfluidsimulation_gb300.engine import DYN_DTYPE, SimulationEngineCUDA
+
+    torch.cuda.set_device(local)
+    scene = workload_scene(args.workload, args.steps)
+    n, s = scene.n, scene.s
+    eng = SimulationEngineCUDA(local)
+    eng.initialize(scene)
+    stream = torch.cuda.ExternalStream(eng.stream_handle(), device=torch.device("cuda", local))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    # warm-up (also builds the step graph)
+    eng.update(scene.dt, args.warmup)
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    barrier(pg)
+    torch.cuda.synchronize()
+    clocks.start()
+    wall0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()                       # L2 flush between timed steps
+            starts[k].record(stream)
+            eng.update_async(scene.dt, 1)
+            ends[k].record(stream)
+    eng.synchronize()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    barrier(pg)
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    total_s = sum(step_ms) / 1000.0
+    total_s = max_over_ranks(pg, total_s, local)
+    value = world * n * args.steps / total_s
+
+    # per-stage times over the same number of steps (events around each stage)
+    eng.set_timing(True)
+    stage_sum = np.zeros(5)
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        eng.update(scene.dt, 1)
+        stage_sum += eng.kernel_times()
+    eng.set_timing(False)
+    stage_ms = stage_sum / args.steps
+    dom = int(np.argmax(stage_ms))
+    dom_name = STAGES[dom]
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes(dom_name, n, s) / (stage_ms[dom] * 1e-3) / 1e9
+    traffic = profiled_traffic(dom_name, args.workload)
+
+    # e2e through the C ABI with host buffers: upload state, one step, read back
+    pinned_in = torch.empty(n * 32, dtype=torch.uint8, pin_memory=True)
+    pinned_out = torch.empty(n * 32, dtype=torch.uint8, pin_memory=True)
+    host_in = pinned_in.numpy().view(DYN_DTYPE)
+    host_out = pinned_out.numpy().view(DYN_DTYPE)
+    eng.read_dynamic(host_in)
+    e2e_steps = max(1, min(args.steps, 10))
+    barrier(pg)
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        eng.write_dynamic(host_in)
+        eng.update(scene.dt, 1)
+        eng.read_dynamic(host_out)
+        host_in, host_out = host_out, host_in
+    e2e_s = max_over_ranks(pg, time.perf_counter() - t0, local)
+    e2e_value = world * n * e2e_steps / e2e_s
+
+    line = {
+        "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total_s / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded SplitMix64 dam break, reference generators)",
+        "config": {"workload": scene.name, "particles": n, "static_particles": s, "h": scene.params.h,
+                   "dt": scene.dt, "buckets": 2 * n, "l2": "flushed (256 MiB write) before every timed step",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "stage_ms": dict(zip(STAGES, [round(float(x), 5) for x in stage_ms])),
+        "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                     "alg_bytes_per_launch": alg_bytes(dom_name, n, s)},
+        "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": 32 * n,
+                "d2h_bytes_per_step": 32 * n, "steps": e2e_steps},
+        "gpu_launches": 5 * args.steps,
+        "clocks": clk,
+        "wall_s_timed_region": wall,
+    }
+    return line, scene
+
+
+def profiled_traffic(stage: str, workload: str):
+    """DRAM bytes per launch of the kernel from the committed ncu summary
+    (profiles/ncu_traffic.txt, lines "workload stage bytes_per_launch")."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for ln in f:
+            parts = ln.split()
+            if len(parts) >= 3 and parts[0] == workload and parts[1] == stage:
+                try:
+                    return float(parts[2])
+                except ValueError:
+                    return None
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="dam_break_1m",
+                    choices=["dam_break_1m", "dam_break_16k", "pool_drop_8m", "batched", "served"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+
+    from sphfluidsimulation_gb300 import build
+    build.build()
+    world, rank, local, pg = dist_setup(args)
+    if args.workload in ("batched", "served"):
+        from sphfluidsimulation_gb300 import bench_forms
+        line = bench_forms.run(args, world, rank, local, pg)
+        scene = None
+    else:
+        line, scene = run_plain(args, world, rank, local, pg)
+    if rank == 0:
+        if scene is not None and not args.no_cpu_baseline and world == 1:
+            threads = os.cpu_count() or 1
+            per_step_s = scene.n / 3.0e6
+            steps = max(1, min(5, int(20.0 / max(per_step_s, 1e-3))))
+            v, secs = cpu_baseline(scene, steps, 1, threads)
+            line["cpu_baseline"] = {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                                    "sample": f"{scene.name}: {scene.n} particles, {steps} steps after 1 warm-up "
+                                              f"({secs:.1f} s), oracle port of the reference CPU engine"}
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

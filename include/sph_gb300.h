@@ -1,0 +1,246 @@
+/*
+ * sph_gb300.h -- C ABI of the GB300 SPH step engine.
+ *
+ * A drop-in third engine behind the reference's engine interface
+ * (Murk42/SPHFluidSimulation, SPHFluidSimulation/include/SPH/Core/
+ * SimulationEngine.h:35-76).  Each entry point below names the reference
+ * member it replaces.  All functions return sph_status and never abort; all
+ * pointers are plain host pointers unless the name says _device.
+ *
+ * Particle layout on the boundary is the reference's 32-byte DynamicParticle
+ * (SPHFluidSimulation/include/SPH/Core/Particles.h:9-17): position, pressure,
+ * velocity, hash.  Readback is in the caller's input order.
+ *
+ * Threading: an engine, batch or server object is used by one host thread at
+ * a time (or under the caller's lock).  Different objects are independent.
+ */
+#ifndef SPH_GB300_H
+#define SPH_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define SPH_API __attribute__((visibility("default")))
+#else
+#define SPH_API
+#endif
+
+typedef enum sph_status {
+    SPH_OK = 0,
+    SPH_ERR_INVALID_ARGUMENT = 1,   /* null pointer, zero h, bad sizes         */
+    SPH_ERR_NOT_INITIALIZED = 2,    /* Update before Initialize (ECPU:422-426) */
+    SPH_ERR_CUDA = 3,               /* a CUDA runtime call failed              */
+    SPH_ERR_OUT_OF_MEMORY = 4,      /* device allocation failed                */
+    SPH_ERR_DEVICE_TIMEOUT = 5,     /* a bounded device wait ran out           */
+    SPH_ERR_CAPACITY = 6,           /* exceeds a fixed limit of the object     */
+    SPH_ERR_BUDGET = 7,             /* HBM budget of a server exhausted        */
+    SPH_ERR_NOT_FOUND = 8           /* unknown scene / job id                  */
+} sph_status;
+
+/* The scene-supplied fields of ParticleBehaviourParameters
+ * (SPHFluidSimulation/include/SPH/Core/Particles.h:19-37; filled from the
+ * scene JSON by SceneBlueprint.cpp:15-33).  selfDensity and the smoothing
+ * kernel constant are derived by the engine as SimulationEngineCPU.cpp:406-407
+ * does. */
+typedef struct sph_params {
+    float particle_mass;
+    float gas_constant;
+    float elasticity;              /* carried, unused by the step (as in the reference) */
+    float viscosity;
+    float gravity_x, gravity_y, gravity_z;
+    float rest_density;
+    float max_interaction_distance; /* h: smoothing radius and cell size */
+} sph_params;
+
+/* Reference DynamicParticle, 32 bytes (Particles.h:9-17). */
+typedef struct sph_dynamic_particle {
+    float position[3];
+    float pressure;
+    float velocity[3];
+    uint32_t hash;                 /* bucket key of the position (SF:644-645) */
+} sph_dynamic_particle;
+
+/* Reference StaticParticle, 16 bytes (Particles.h:19-23). */
+typedef struct sph_static_particle {
+    float position[3];
+    float pressure;
+} sph_static_particle;
+
+typedef struct sph_engine sph_engine;
+
+/* Human-readable name of a status code. */
+SPH_API const char* sph_status_string(sph_status status);
+
+/* Last error message recorded on this host thread (empty if none). */
+SPH_API const char* sph_last_error(void);
+
+/* Engine constructor: replaces SimulationEngineCPU(threadCount)
+ * (SimulationEngineCPU.cpp:351-360).  device = CUDA ordinal. */
+SPH_API sph_status sph_engine_create(sph_engine** out, int device);
+
+/* Destructor (SimulationEngineCPU.cpp:361-364).  Frees all device memory. */
+SPH_API sph_status sph_engine_destroy(sph_engine* engine);
+
+/* SimulationEngine::Clear (SimulationEngineCPU.cpp:365-395): drops the
+ * scene, keeps the device arena for reuse. */
+SPH_API sph_status sph_engine_clear(sph_engine* engine);
+
+/* SimulationEngine::Initialize (SimulationEngineCPU.cpp:396-419) with the
+ * SceneBlueprint flattened to arrays (SceneBlueprint.h:23-51):
+ *   dyn_pos     n x 3 floats, the "dynamic" layer positions
+ *   dyn_vel     n x 3 floats or NULL (the reference starts at rest)
+ *   static_pos  s x 3 floats, the "static" layer positions (may be NULL if s=0)
+ *   triangles   t x 9 floats, boundary mesh triangles (may be NULL if t=0)
+ *   reorder_time_interval  the scene's "reorderTimeInterval" (accepted; this
+ *               engine keeps particles physically sorted every step)
+ * Bucket count is 2n (SimulationEngineCPU.cpp:486), static buckets s. */
+SPH_API sph_status sph_engine_initialize(sph_engine* engine, const sph_params* params,
+                                         const float* dyn_pos, const float* dyn_vel, uint32_t n,
+                                         const float* static_pos, uint32_t s,
+                                         const float* triangles, uint32_t t,
+                                         float reorder_time_interval);
+
+/* SimulationEngine::Update (SimulationEngineCPU.cpp:420-459): advance
+ * `steps` steps of dt.  Returns when the device work is complete (the
+ * reference's CPU engine queues asynchronously and may drop the call; this
+ * engine never drops a call). */
+SPH_API sph_status sph_engine_update(sph_engine* engine, float dt, uint32_t steps);
+
+/* Same, but returns once the work is queued on the engine's stream. */
+SPH_API sph_status sph_engine_update_async(sph_engine* engine, float dt, uint32_t steps);
+
+/* Waits for queued work; reports SPH_ERR_DEVICE_TIMEOUT if a bounded device
+ * wait expired during it. */
+SPH_API sph_status sph_engine_synchronize(sph_engine* engine);
+
+/* GetDynamicParticlesBufferManager()->LockRead() readback
+ * (OfflineCPUParticleBufferManager.cpp:109-115): the current particles in
+ * the caller's input order (out has n entries). */
+SPH_API sph_status sph_engine_read_dynamic(sph_engine* engine, sph_dynamic_particle* out);
+
+/* LockWrite()-style upload: replaces every particle's position and velocity
+ * (input order; pressure and hash are ignored) and re-sorts. */
+SPH_API sph_status sph_engine_write_dynamic(sph_engine* engine, const sph_dynamic_particle* in);
+
+/* GetStaticParticlesBufferManager()->LockRead(): static particles in bucket
+ * order, plus the s+1 bucket-start table (may be NULL). */
+SPH_API sph_status sph_engine_read_static(sph_engine* engine, sph_static_particle* out, uint32_t* bucket_starts);
+
+/* The dynamic bucket table after the last step, in the reference's meaning
+ * (hashMap, SimulationEngineCPU.cpp:486-487): bucket_starts has 2n+1 entries,
+ * bucket b holds slots [bucket_starts[b], bucket_starts[b+1]); slot_ids has n
+ * entries, the input index of the particle in each slot (the reference's
+ * particleMap followed through its init permutation).  Either may be NULL. */
+SPH_API sph_status sph_engine_read_buckets(sph_engine* engine, uint32_t* bucket_starts, uint32_t* slot_ids);
+
+/* GetSimulationTime (SimulationEngineCPU.h:23). */
+SPH_API sph_status sph_engine_simulation_time(sph_engine* engine, double* seconds);
+
+/* SystemImplementationName (SimulationEngineCPU.h:19): "CUDA-sm_103a". */
+SPH_API const char* sph_engine_implementation_name(void);
+
+/* Particle counts: which = 0 dynamic, 1 static, 2 dynamic buckets, 3 triangles. */
+SPH_API sph_status sph_engine_count(sph_engine* engine, int which, uint64_t* value);
+
+/* Debug output: when on, each step also stores the acceleration
+ * F/rho + g of every particle; read it (input order, n x 3) after a step. */
+SPH_API sph_status sph_engine_record_acceleration(sph_engine* engine, int on);
+SPH_API sph_status sph_engine_read_acceleration(sph_engine* engine, float* out);
+
+/* Per-kernel device time of the last update, milliseconds, in the order
+ * density, force, scan, scatter, gather (5 values).  Recorded only while
+ * timing is on (it adds events to each step). */
+SPH_API sph_status sph_engine_set_timing(sph_engine* engine, int on);
+SPH_API sph_status sph_engine_kernel_times(sph_engine* engine, float* ms, int count);
+
+/* The engine's CUDA stream (a cudaStream_t), for callers that order their
+ * own work or timing events with the engine's launches. */
+SPH_API sph_status sph_engine_get_stream(sph_engine* engine, void** stream);
+
+/* ---- the counting sort stage on its own ---------------------------------
+ * Hash + count + scan + stable scatter of n positions into `buckets` buckets
+ * with cell size h, on the device (SF:321-356 with the serial scan of
+ * SimulationEngineCPU.cpp:245-253).  Outputs (each may be NULL):
+ *   keys    n     key of each input position, GetHash(GetCell(p)) % buckets
+ *   counts  buckets  particles per bucket
+ *   starts  buckets+1  bucket start slots, starts[buckets] = n
+ *   order   n     input index of the particle in each slot (stable: ties keep
+ *                 input order) */
+SPH_API sph_status sph_cell_sort(int device, const float* pos, uint32_t n, float h, uint32_t buckets,
+                                 uint32_t* keys, uint32_t* counts, uint32_t* starts, uint32_t* order);
+
+/* ---- batched engine: many scenes advanced by one persistent launch ------ */
+
+typedef struct sph_batch sph_batch;
+
+/* Creates an empty batch on `device`. */
+SPH_API sph_status sph_batch_create(sph_batch** out, int device);
+SPH_API sph_status sph_batch_destroy(sph_batch* batch);
+
+/* Adds a scene (same arguments as sph_engine_initialize plus its dt);
+ * returns its id.  Scenes are uploaded when the batch is finalized. */
+SPH_API sph_status sph_batch_add_scene(sph_batch* batch, const sph_params* params,
+                                       const float* dyn_pos, const float* dyn_vel, uint32_t n,
+                                       const float* static_pos, uint32_t s,
+                                       const float* triangles, uint32_t t, float dt,
+                                       uint32_t* scene_id);
+
+/* Uploads and sorts all scenes, sizes the persistent launch, captures the
+ * step in a CUDA graph. */
+SPH_API sph_status sph_batch_finalize(sph_batch* batch);
+
+/* Advances every scene by `steps` steps (each by its own dt), one persistent
+ * launch per step.  mode 0 = persistent fused step (default), mode 1 = one
+ * launch per stage over all scenes. */
+SPH_API sph_status sph_batch_step(sph_batch* batch, uint32_t steps);
+SPH_API sph_status sph_batch_set_mode(sph_batch* batch, int mode);
+
+/* Reads one scene's particles in its input order. */
+SPH_API sph_status sph_batch_read_scene(sph_batch* batch, uint32_t scene_id, sph_dynamic_particle* out);
+
+/* Sum of particles over scenes; the persistent grid size chosen. */
+SPH_API sph_status sph_batch_info(sph_batch* batch, uint64_t* total_particles, uint32_t* grid_ctas,
+                                  uint32_t* threads_per_cta);
+
+/* ---- server: continuous batching of simulation jobs -------------------- */
+
+typedef struct sph_server sph_server;
+
+/* hbm_budget_bytes bounds the resident state of admitted jobs; max_slots
+ * bounds how many jobs share one step. */
+SPH_API sph_status sph_server_create(sph_server** out, int device, uint64_t hbm_budget_bytes,
+                                     uint32_t max_slots);
+SPH_API sph_status sph_server_destroy(sph_server* server);
+
+/* Queues a job (copied): a scene plus a horizon in steps.  Rejects with
+ * SPH_ERR_BUDGET if the job alone can never fit the budget and
+ * SPH_ERR_INVALID_ARGUMENT for malformed jobs. */
+SPH_API sph_status sph_server_submit(sph_server* server, const sph_params* params,
+                                     const float* dyn_pos, uint32_t n,
+                                     const float* static_pos, uint32_t s, float dt,
+                                     uint32_t steps, uint64_t* job_id);
+
+/* Runs one scheduling round: admits queued jobs that fit, advances every
+ * admitted job by up to `chunk_steps` steps in one batched launch sequence,
+ * retires finished jobs.  *active and *queued report the state afterwards. */
+SPH_API sph_status sph_server_poll(sph_server* server, uint32_t chunk_steps, uint32_t* active,
+                                   uint32_t* queued);
+
+/* Retrieves a finished job's particles (input order, n entries) and
+ * densities (n floats, rho = p/k + rho0); may be NULL.  Returns
+ * SPH_ERR_NOT_FOUND while the job is unfinished. */
+SPH_API sph_status sph_server_result(sph_server* server, uint64_t job_id, sph_dynamic_particle* out,
+                                     float* density);
+
+/* Bytes of device state a job of n dynamic and s static particles holds. */
+SPH_API uint64_t sph_server_job_bytes(uint32_t n, uint32_t s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPH_GB300_H */

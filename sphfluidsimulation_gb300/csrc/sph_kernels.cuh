@@ -1,0 +1,591 @@
+// sph_kernels.cuh -- the per-stage device routines of one SPH step.
+//
+// Each stage is a __device__ routine over one Tile (one CTA's slots of one
+// scene), so the same code runs from a plain per-stage kernel and from the
+// persistent fused step kernel.  Reference counterparts (SF =
+// SPHFluidSimulation/source/SPH/Kernels/SPHFunctions.cpp):
+//   hash_count_tile      SF:321-331  key + warp-aggregated bucket count
+//   scan_tile            SF:227-294  single-pass decoupled-lookback scan
+//   scatter_tile         SF:346-356  slot = bucket start + arrival rank
+//   gather_tile          SF:332-345  stable rank inside the bucket + SoA move
+//   density_tile         SF:358-501  27-bucket density / pressure pass
+//   force_tile           SF:503-656  27-bucket force, integrate, rehash
+//
+// Data layout (struct of arrays, sorted by bucket every step):
+//   pos[i] = (x, y, z, input index as bits)
+//   vel[i] = (vx, vy, vz, pressure)       pressure written by the density pass
+#pragma once
+#include "sph_common.cuh"
+
+namespace sph {
+
+constexpr int kTileThreads = 128;          // slots per tile = threads per CTA
+constexpr int kScanThreads = kTileThreads;  // the scan runs inside the fused kernel too
+constexpr int kScanItems = 16;             // per thread
+constexpr int kScanTile = kScanThreads * kScanItems;
+constexpr uint32_t kSpinLimit = 1u << 21;  // bounded waits: ~1-2 s with backoff
+
+struct StepArgs {
+    const Tile* tiles;          // dynamic-particle tiles
+    uint32_t num_tiles;
+    const SceneDesc* scenes;
+    float4* pos;                // sorted state
+    float4* vel;
+    float4* pos_tmp;            // unsorted output of the force pass
+    float4* vel_tmp;
+    uint32_t* key;              // local bucket of the new position, per tmp slot
+    uint32_t* arrival;          // arrival rank inside the bucket, per tmp slot
+    uint32_t* perm;             // slot -> tmp slot (arrival order)
+    uint32_t* count;            // bucket counters, zero between steps
+    uint32_t* start;            // exclusive scan of count
+    uint32_t scan_len;          // entries of count/start scanned
+    unsigned long long* scan_status;
+    uint32_t* scan_ticket;
+    const float4* spos;         // sorted static particles
+    const uint32_t* sstart;     // static bucket table (global scan)
+    const float* tris;          // 9 floats per triangle
+    float4* accel;              // optional: acceleration per sorted slot (.w unused)
+    uint32_t* err;              // device status word
+    uint32_t* bar_count;        // grid barrier (persistent kernel only)
+    uint32_t* bar_gen;
+};
+
+// ---- small helpers ---------------------------------------------------------
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+
+__device__ __forceinline__ void set_error(uint32_t* err, uint32_t bit) { atomicOr(err, bit); }
+
+// Adds 1 to counter[g] for every valid lane, one atomic per distinct g in the
+// warp; returns this lane's arrival rank (the pre-increment value plus the
+// number of lower lanes with the same g).
+__device__ __forceinline__ uint32_t warp_aggregated_increment(uint32_t* counter, uint32_t g, bool valid)
+{
+    const unsigned active = __ballot_sync(0xffffffffu, valid);
+    uint32_t rank = 0;
+    if (valid) {
+        const unsigned peers = __match_any_sync(active, g);
+        const int leader = __ffs(peers) - 1;
+        const uint32_t lane = lane_id();
+        uint32_t base = 0;
+        if ((int)lane == leader) base = atomicAdd(counter + g, (uint32_t)__popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        rank = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+    }
+    return rank;
+}
+
+// The 9 expanded coordinates of a cell's 3x3x3 neighbourhood: the Morton
+// code of (c + d) is ex[dx] + ey[dy] + ez[dz] (SF:88-97 with the & 0x3FF
+// mask, cells wrapping as unsigned like SF:386-395).  Kept in registers and
+// picked with selects, so no local-memory array is needed.
+struct Neighbourhood {
+    uint32_t ex0, ex1, ex2, ey0, ey1, ey2, ez0, ez1, ez2;
+};
+
+__device__ __forceinline__ Neighbourhood neighbourhood(float x, float y, float z, float h)
+{
+    const uint32_t cx = cell_coord(x, h), cy = cell_coord(y, h), cz = cell_coord(z, h);
+    Neighbourhood nb;
+    nb.ex0 = expand_bits((cx - 1u) & 0x3FFu);
+    nb.ex1 = expand_bits(cx & 0x3FFu);
+    nb.ex2 = expand_bits((cx + 1u) & 0x3FFu);
+    nb.ey0 = expand_bits((cy - 1u) & 0x3FFu) * 2u;
+    nb.ey1 = expand_bits(cy & 0x3FFu) * 2u;
+    nb.ey2 = expand_bits((cy + 1u) & 0x3FFu) * 2u;
+    nb.ez0 = expand_bits((cz - 1u) & 0x3FFu) * 4u;
+    nb.ez1 = expand_bits(cz & 0x3FFu) * 4u;
+    nb.ez2 = expand_bits((cz + 1u) & 0x3FFu) * 4u;
+    return nb;
+}
+
+__device__ __forceinline__ uint32_t pick3(int k, uint32_t v0, uint32_t v1, uint32_t v2)
+{
+    return k == 0 ? v0 : (k == 1 ? v1 : v2);
+}
+
+// Morton code of neighbour cell (a, b, c) in {0,1,2}^3, x outermost as in
+// the reference's loops (SF:392-395).
+__device__ __forceinline__ uint32_t neighbour_hash(const Neighbourhood& nb, int a, int b, int c)
+{
+    return pick3(a, nb.ex0, nb.ex1, nb.ex2) + pick3(b, nb.ey0, nb.ey1, nb.ey2) + pick3(c, nb.ez0, nb.ez1, nb.ez2);
+}
+
+// RandomDirection (SF:140-155): sin-hash noise evaluated in double as the
+// reference's C++ build does; used only for coincident particles.
+__device__ __noinline__ inline float3 random_direction(float x)
+{
+    double s_in = (double)(x * 112.9898f);
+    double v = sin(s_in) * (double)43758.5453f;
+    float noise = (float)(v - trunc(v));
+    float theta = noise * 2.0f * 3.1415f;
+    float z = noise * 2.0f - 1.0f;
+    double sn = sin((double)theta), cs = cos((double)theta);
+    double z2 = sqrt((double)(1.0f - z * z));
+    return make_float3((float)(z2 * cs), (float)(z2 * sn), z);
+}
+
+// ClosestPointOnTriangle + CalculateTriangleForce (SF:156-223).
+__device__ __noinline__ inline float3 triangle_force(float3 p, const float* tri)
+{
+    const float3 a = make_float3(tri[0], tri[1], tri[2]);
+    const float3 b = make_float3(tri[3], tri[4], tri[5]);
+    const float3 c = make_float3(tri[6], tri[7], tri[8]);
+    auto sub = [](float3 u, float3 v) { return make_float3(u.x - v.x, u.y - v.y, u.z - v.z); };
+    auto dot = [](float3 u, float3 v) { return __fadd_rn(__fadd_rn(__fmul_rn(u.x, v.x), __fmul_rn(u.y, v.y)), __fmul_rn(u.z, v.z)); };
+    auto axpy = [](float3 o, float3 u, float s) { return make_float3(__fadd_rn(o.x, __fmul_rn(u.x, s)), __fadd_rn(o.y, __fmul_rn(u.y, s)), __fadd_rn(o.z, __fmul_rn(u.z, s))); };
+    float3 q;
+    const float3 ab = sub(b, a), ac = sub(c, a), ap = sub(p, a);
+    const float d1 = dot(ab, ap), d2 = dot(ac, ap);
+    const float3 bp = sub(p, b);
+    const float d3 = dot(ab, bp), d4 = dot(ac, bp);
+    const float3 cp = sub(p, c);
+    const float d5 = dot(ab, cp), d6 = dot(ac, cp);
+    const float vc = __fsub_rn(__fmul_rn(d1, d4), __fmul_rn(d3, d2));
+    const float vb = __fsub_rn(__fmul_rn(d5, d2), __fmul_rn(d1, d6));
+    const float va = __fsub_rn(__fmul_rn(d3, d6), __fmul_rn(d5, d4));
+    if (d1 <= 0.f && d2 <= 0.f) q = a;
+    else if (d3 >= 0.f && d4 <= d3) q = b;
+    else if (d6 >= 0.f && d5 <= d6) q = c;
+    else if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) q = axpy(a, ab, __fdiv_rn(d1, __fsub_rn(d1, d3)));
+    else if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) q = axpy(a, ac, __fdiv_rn(d2, __fsub_rn(d2, d6)));
+    else if (va <= 0.f && __fsub_rn(d4, d3) >= 0.f && __fsub_rn(d5, d6) >= 0.f) {
+        const float e = __fsub_rn(d4, d3);
+        q = axpy(b, sub(c, b), __fdiv_rn(e, __fadd_rn(e, __fsub_rn(d5, d6))));
+    } else {
+        const float denom = __fdiv_rn(1.f, __fadd_rn(__fadd_rn(va, vb), vc));
+        q = axpy(axpy(a, ab, __fmul_rn(vb, denom)), ac, __fmul_rn(vc, denom));
+    }
+    const float3 to = sub(q, p);
+    const float dist = __fsqrt_rn(dot(to, to));
+    if (dist > 2.5f) return make_float3(0.f, 0.f, 0.f);
+    const float t = __fsub_rn(__fdiv_rn(1.f, __fdiv_rn(dist, 2.5f)), 1.f);
+    const float amp = __fmul_rn(t, t);
+    float3 dir = make_float3(__fdiv_rn(-to.x, dist), __fdiv_rn(-to.y, dist), __fdiv_rn(-to.z, dist));
+    return make_float3(__fmul_rn(__fmul_rn(dir.x, amp), 50.f), __fmul_rn(__fmul_rn(dir.y, amp), 50.f),
+                       __fmul_rn(__fmul_rn(dir.z, amp), 50.f));
+}
+
+// ---- stage: hash + count ---------------------------------------------------
+
+// key[i] = GetHash(GetCell(pos[i])) % buckets; count[q_off + key]++ with one
+// atomic per distinct key per warp; arrival[i] = rank among that key's adds.
+__device__ __forceinline__ void hash_count_tile(const Tile& tile, const SceneDesc* scenes, const float4* pos,
+                                                uint32_t* key, uint32_t* arrival, uint32_t* count)
+{
+    const SceneDesc& sc = scenes[tile.scene];
+    const uint32_t i = tile.begin + threadIdx.x;
+    const bool valid = i < tile.end;
+    uint32_t g = 0, k = 0;
+    if (valid) {
+        const float4 p = pos[i];
+        k = fast_mod(cell_hash(p.x, p.y, p.z, sc.h), sc.fm_b);
+        g = sc.q_off + k;
+    }
+    const uint32_t r = warp_aggregated_increment(count, g, valid);
+    if (valid) {
+        key[i] = k;
+        arrival[i] = r;
+    }
+}
+
+// ---- stage: exclusive scan (decoupled look-back) ---------------------------
+//
+// Merrill & Garland, "Single-pass Parallel Prefix Scan with Decoupled
+// Look-back" (NVIDIA TR, 2016).  Tile ids come from a ticket counter so a
+// tile only ever waits on tiles already claimed by running CTAs.  Status
+// word: bits 32-33 = 1 aggregate, 2 inclusive prefix; low 32 bits = value.
+// Every wait is bounded; on expiry the error word is set and the scan
+// finishes with the value it has (the host reports SPH_ERR_DEVICE_TIMEOUT).
+// Writes start[i] = sum(count[0..i)), then zeroes count[i].
+
+struct ScanSmem {
+    uint4 items[kScanThreads * kScanItems / 4];
+    uint32_t warp_sums[kScanThreads / 32];
+    uint32_t tile;
+    uint32_t exclusive;
+};
+
+__device__ __forceinline__ unsigned long long load_status(const unsigned long long* p)
+{
+    return *(const volatile unsigned long long*)p;
+}
+
+__device__ inline void scan_tile(uint32_t tile, uint32_t* count, uint32_t* start, uint32_t len,
+                          unsigned long long* status, uint32_t* err, ScanSmem& sm)
+{
+    const uint32_t base = tile * (uint32_t)kScanTile;
+    const uint32_t t = threadIdx.x;
+    // striped vector loads into shared memory
+#pragma unroll
+    for (int k = 0; k < kScanItems / 4; ++k) {
+        const uint32_t v = (uint32_t)k * kScanThreads + t;        // uint4 index in tile
+        const uint32_t e = base + v * 4u;
+        uint4 q;
+        if (e + 4u <= len) {
+            q = *reinterpret_cast<const uint4*>(count + e);
+        } else {
+            q.x = e + 0u < len ? count[e + 0u] : 0u;
+            q.y = e + 1u < len ? count[e + 1u] : 0u;
+            q.z = e + 2u < len ? count[e + 2u] : 0u;
+            q.w = e + 3u < len ? count[e + 3u] : 0u;
+        }
+        sm.items[v] = q;
+    }
+    __syncthreads();
+    // each thread owns kScanItems consecutive items
+    uint32_t vals[kScanItems];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems / 4; ++k) {
+        const uint4 q = sm.items[t * (kScanItems / 4) + k];
+        vals[4 * k + 0] = q.x; vals[4 * k + 1] = q.y; vals[4 * k + 2] = q.z; vals[4 * k + 3] = q.w;
+        sum += q.x + q.y + q.z + q.w;
+    }
+    // block-wide exclusive scan of the per-thread sums
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane_id() >= (uint32_t)o) incl += y;
+    }
+    const uint32_t warp = t >> 5;
+    if (lane_id() == 31u) sm.warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane_id() < kScanThreads / 32 ? sm.warp_sums[lane_id()] : 0u;
+        uint32_t wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane_id() >= (uint32_t)o) wi += y;
+        }
+        const uint32_t aggregate = __shfl_sync(0xffffffffu, wi, kScanThreads / 32 - 1);
+        if (lane_id() < kScanThreads / 32) sm.warp_sums[lane_id()] = wi - w;   // exclusive per warp
+        // publish and look back
+        uint32_t exclusive = 0;
+        if (tile == 0) {
+            if (lane_id() == 0)
+                atomicExch(&status[0], (2ull << 32) | (unsigned long long)aggregate);
+        } else {
+            if (lane_id() == 0)
+                atomicExch(&status[tile], (1ull << 32) | (unsigned long long)aggregate);
+            int64_t pred = (int64_t)tile - 1;
+            uint32_t spins = 0;
+            bool timed_out = false;
+            while (true) {
+                const int64_t idx = pred - (int64_t)lane_id();
+                unsigned long long s = idx >= 0 ? load_status(&status[idx]) : (2ull << 32);
+                uint32_t flag = (uint32_t)(s >> 32) & 3u;
+                if (__any_sync(0xffffffffu, flag == 0u) && !timed_out) {
+                    if (++spins > kSpinLimit) {
+                        timed_out = true;
+                        if (lane_id() == 0) set_error(err, DEV_ERR_SCAN_TIMEOUT);
+                    } else {
+                        __nanosleep(spins < 64 ? 32 : 256);
+                    }
+                    continue;
+                }
+                if (flag == 0u) { s = (2ull << 32); flag = 2u; }          // timed out: stop here
+                const unsigned prefix_mask = __ballot_sync(0xffffffffu, flag == 2u);
+                const uint32_t value = (uint32_t)s;
+                if (prefix_mask) {
+                    const int first = __ffs(prefix_mask) - 1;             // nearest inclusive prefix
+                    uint32_t contrib = (int)lane_id() <= first ? value : 0u;
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) contrib += __shfl_xor_sync(0xffffffffu, contrib, o);
+                    exclusive += contrib;
+                    break;
+                }
+                uint32_t contrib = value;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) contrib += __shfl_xor_sync(0xffffffffu, contrib, o);
+                exclusive += contrib;
+                pred -= 32;
+            }
+            if (lane_id() == 0)
+                atomicExch(&status[tile], (2ull << 32) | (unsigned long long)(exclusive + aggregate));
+        }
+        if (lane_id() == 0) sm.exclusive = exclusive;
+    }
+    __syncthreads();
+    uint32_t run = sm.exclusive + sm.warp_sums[warp] + (incl - sum);
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const uint32_t c = vals[k];
+        vals[k] = run;
+        run += c;
+    }
+    // write back through shared memory (striped, vectorised)
+#pragma unroll
+    for (int k = 0; k < kScanItems / 4; ++k)
+        sm.items[t * (kScanItems / 4) + k] = make_uint4(vals[4 * k], vals[4 * k + 1], vals[4 * k + 2], vals[4 * k + 3]);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kScanItems / 4; ++k) {
+        const uint32_t v = (uint32_t)k * kScanThreads + t;
+        const uint32_t e = base + v * 4u;
+        const uint4 q = sm.items[v];
+        if (e + 4u <= len) {
+            *reinterpret_cast<uint4*>(start + e) = q;
+            *reinterpret_cast<uint4*>(count + e) = make_uint4(0u, 0u, 0u, 0u);
+        } else {
+            if (e + 0u < len) { start[e + 0u] = q.x; count[e + 0u] = 0u; }
+            if (e + 1u < len) { start[e + 1u] = q.y; count[e + 1u] = 0u; }
+            if (e + 2u < len) { start[e + 2u] = q.z; count[e + 2u] = 0u; }
+        }
+    }
+    __syncthreads();
+}
+
+// ---- stage: scatter (arrival order) ----------------------------------------
+
+__device__ __forceinline__ void scatter_tile(const Tile& tile, const SceneDesc* scenes, const uint32_t* key,
+                                             const uint32_t* arrival, const uint32_t* start, uint32_t* perm,
+                                             uint32_t* err)
+{
+    const SceneDesc& sc = scenes[tile.scene];
+    const uint32_t i = tile.begin + threadIdx.x;
+    if (i >= tile.end) return;
+    const uint32_t delta = sc.p_off - start[sc.q_off];
+    const uint32_t slot = start[sc.q_off + key[i]] + delta + arrival[i];
+    if (slot - sc.p_off >= sc.n) { set_error(err, DEV_ERR_SLOT_RANGE); return; }
+    perm[slot] = i;
+}
+
+// ---- stage: stable gather --------------------------------------------------
+//
+// Source slot j moves to bucket start + (number of the bucket's members with
+// a smaller source slot), so each bucket keeps the previous slot order: a
+// deterministic, stable counting sort.  Buckets hold a handful of particles,
+// so the rank loop reads a few words from L1.
+constexpr uint32_t kStableRankLimit = 4096;   // larger buckets keep arrival order
+
+__device__ __forceinline__ void gather_tile(const Tile& tile, const SceneDesc* scenes, const uint32_t* key,
+                                            const uint32_t* arrival, const uint32_t* perm, const uint32_t* start,
+                                            const float4* pos_src, const float4* vel_src, float4* pos_dst,
+                                            float4* vel_dst, uint32_t* err)
+{
+    const SceneDesc& sc = scenes[tile.scene];
+    const uint32_t j = tile.begin + threadIdx.x;
+    if (j >= tile.end) return;
+    const uint32_t delta = sc.p_off - start[sc.q_off];
+    const uint32_t g = sc.q_off + key[j];
+    const uint32_t b0 = start[g] + delta;
+    const uint32_t e0 = start[g + 1] + delta;
+    if (b0 - sc.p_off > sc.n || e0 - sc.p_off > sc.n || e0 < b0) { set_error(err, DEV_ERR_BUCKET_RANGE); return; }
+    uint32_t rank = 0;
+    if (e0 - b0 <= kStableRankLimit) {
+        for (uint32_t t = b0; t < e0; ++t) rank += (perm[t] < j) ? 1u : 0u;
+    } else {
+        rank = arrival[j];
+    }
+    const uint32_t dst = b0 + rank;
+    if (dst >= e0) { set_error(err, DEV_ERR_SLOT_RANGE); return; }
+    pos_dst[dst] = pos_src[j];
+    vel_dst[dst] = vel_src[j];
+}
+
+// Squared distance with a fixed rounding sequence, so every kernel that
+// inlines it produces the same bits.
+__device__ __forceinline__ float dist2(const float4& q, const float4& p)
+{
+    const float dx = __fsub_rn(q.x, p.x), dy = __fsub_rn(q.y, p.y), dz = __fsub_rn(q.z, p.z);
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+// ---- stage: density / pressure ---------------------------------------------
+//
+// UpdateParticlePressure (SF:358-501): for the 27 buckets of the cell
+// neighbourhood (bucket ids repeat if cells collide, as in the reference),
+// sum (h - r)^3 over dynamic neighbours (self skipped) and static neighbours
+// within h; rho = selfDensity + (sum_d m + sum_s m) C; p = k (rho - rho0).
+__device__ __forceinline__ void density_tile(const Tile& tile, const SceneDesc* scenes, const float4* __restrict__ pos,
+                                             float4* __restrict__ vel, const uint32_t* __restrict__ start,
+                                             const float4* __restrict__ spos, const uint32_t* __restrict__ sstart)
+{
+    const SceneDesc& sc = scenes[tile.scene];
+    const uint32_t i = tile.begin + threadIdx.x;
+    if (i >= tile.end) return;
+    const float h = sc.h, h2 = sc.h2;
+    const float4 p = pos[i];
+    const Neighbourhood nb = neighbourhood(p.x, p.y, p.z, h);
+    const uint32_t delta = sc.p_off - __ldg(start + sc.q_off);
+    const uint32_t sdelta = sc.s ? sc.s_off - __ldg(sstart + sc.sq_off) : 0u;
+    float sum_d = 0.f, sum_s = 0.f;
+#pragma unroll 1
+    for (int a = 0; a < 3; ++a)
+#pragma unroll 1
+        for (int b = 0; b < 3; ++b)
+#pragma unroll 1
+            for (int c = 0; c < 3; ++c) {
+                const uint32_t hsh = neighbour_hash(nb, a, b, c);
+                const uint32_t bk = sc.q_off + fast_mod(hsh, sc.fm_b);
+                const uint32_t beg = max(__ldg(start + bk) + delta, sc.p_off);
+                const uint32_t end = min(__ldg(start + bk + 1) + delta, sc.p_off + sc.n);
+                for (uint32_t j = beg; j < end; ++j) {
+                    const float4 q = __ldg(pos + j);
+                    const float r2 = dist2(q, p);
+                    if (r2 <= h2 && j != i) {
+                        const float r = __fsqrt_rn(r2);
+                        if (r < h) {
+                            const float w = __fsub_rn(h, r);
+                            sum_d = __fmaf_rn(__fmul_rn(w, w), w, sum_d);
+                        }
+                    }
+                }
+                if (sc.s) {
+                    const uint32_t sb = sc.sq_off + fast_mod(hsh, sc.fm_s);
+                    const uint32_t sbeg = max(__ldg(sstart + sb) + sdelta, sc.s_off);
+                    const uint32_t send = min(__ldg(sstart + sb + 1) + sdelta, sc.s_off + sc.s);
+                    for (uint32_t j = sbeg; j < send; ++j) {
+                        const float4 q = __ldg(spos + j);
+                        const float r2 = dist2(q, p);
+                        if (r2 <= h2) {
+                            const float r = __fsqrt_rn(r2);
+                            if (r < h) {
+                                const float w = __fsub_rn(h, r);
+                                sum_s = __fmaf_rn(__fmul_rn(w, w), w, sum_s);
+                            }
+                        }
+                    }
+                }
+            }
+    const float rho = __fadd_rn(sc.self_density,
+                                __fmul_rn(__fadd_rn(__fmul_rn(sum_d, sc.mass), __fmul_rn(sum_s, sc.mass)), sc.kc));
+    const float pressure = __fmul_rn(sc.gas, __fsub_rn(rho, sc.rho0));
+    reinterpret_cast<float*>(vel + i)[3] = pressure;
+}
+
+// ---- stage: force + integrate + rehash -------------------------------------
+//
+// UpdateParticleDynamics (SF:503-656): pressure force dir (p_i + p_j) W1 and
+// viscosity (v_j - v_i) W2 over dynamic neighbours; dir |p_i| W1 over static
+// neighbours (their viscosity term is multiplied by 0 in the reference,
+// SF:629, and is omitted); scale by m / (2 rho_i) C and mu m C; add triangle
+// forces; a = F / rho_i + g; semi-implicit Euler; new key; count.
+template <bool kRecordAccel>
+__device__ __forceinline__ void force_tile(const Tile& tile, const SceneDesc* scenes, const float4* __restrict__ pos,
+                                           const float4* __restrict__ vel, const uint32_t* __restrict__ start,
+                                           const float4* __restrict__ spos, const uint32_t* __restrict__ sstart,
+                                           const float* __restrict__ tris, float4* __restrict__ pos_out,
+                                           float4* __restrict__ vel_out, uint32_t* __restrict__ key_out,
+                                           uint32_t* __restrict__ arrival, uint32_t* count, float4* accel)
+{
+    const SceneDesc& sc = scenes[tile.scene];
+    const uint32_t i = tile.begin + threadIdx.x;
+    const bool valid = i < tile.end;
+    uint32_t g = 0, k = 0;
+    if (valid) {
+        const float h = sc.h, h2 = sc.h2;
+        const float4 p = pos[i];
+        const float4 v = vel[i];
+        const float pi = v.w;
+        const float rho = __fadd_rn(__fdiv_rn(pi, sc.gas), sc.rho0);
+        const Neighbourhood nb = neighbourhood(p.x, p.y, p.z, h);
+        const uint32_t delta = sc.p_off - __ldg(start + sc.q_off);
+        const uint32_t sdelta = sc.s ? sc.s_off - __ldg(sstart + sc.sq_off) : 0u;
+        float3 fp = make_float3(0.f, 0.f, 0.f);   // dynamic pressure
+        float3 fv = make_float3(0.f, 0.f, 0.f);   // dynamic viscosity
+        float3 fs = make_float3(0.f, 0.f, 0.f);   // static pressure
+        const float api = fabsf(pi);
+#pragma unroll 1
+        for (int a = 0; a < 3; ++a)
+#pragma unroll 1
+            for (int b = 0; b < 3; ++b)
+#pragma unroll 1
+                for (int c = 0; c < 3; ++c) {
+                    const uint32_t hsh = neighbour_hash(nb, a, b, c);
+                    const uint32_t bk = sc.q_off + fast_mod(hsh, sc.fm_b);
+                    const uint32_t beg = max(__ldg(start + bk) + delta, sc.p_off);
+                    const uint32_t end = min(__ldg(start + bk + 1) + delta, sc.p_off + sc.n);
+                    for (uint32_t j = beg; j < end; ++j) {
+                        const float4 q = __ldg(pos + j);
+                        float dx = __fsub_rn(q.x, p.x), dy = __fsub_rn(q.y, p.y), dz = __fsub_rn(q.z, p.z);
+                        const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                        if (r2 <= h2 && j != i) {
+                            const float r = __fsqrt_rn(r2);
+                            if (r < h) {
+                                const float4 u = __ldg(vel + j);
+                                if (r2 == 0.f || r == 0.f) {
+                                    const float3 d = random_direction((float)__float_as_uint(p.w));
+                                    dx = d.x; dy = d.y; dz = d.z;
+                                } else {
+                                    const float inv = __frcp_rn(r);
+                                    dx = __fmul_rn(dx, inv); dy = __fmul_rn(dy, inv); dz = __fmul_rn(dz, inv);
+                                }
+                                const float w = __fsub_rn(h, r);
+                                const float w1 = __fmul_rn(__fmul_rn(-3.f, w), w);
+                                const float w2 = __fmul_rn(6.f, w);
+                                const float pp = __fmul_rn(__fadd_rn(pi, u.w), w1);
+                                fp.x = __fmaf_rn(dx, pp, fp.x);
+                                fp.y = __fmaf_rn(dy, pp, fp.y);
+                                fp.z = __fmaf_rn(dz, pp, fp.z);
+                                fv.x = __fmaf_rn(__fsub_rn(u.x, v.x), w2, fv.x);
+                                fv.y = __fmaf_rn(__fsub_rn(u.y, v.y), w2, fv.y);
+                                fv.z = __fmaf_rn(__fsub_rn(u.z, v.z), w2, fv.z);
+                            }
+                        }
+                    }
+                    if (sc.s) {
+                        const uint32_t sb = sc.sq_off + fast_mod(hsh, sc.fm_s);
+                        const uint32_t sbeg = max(__ldg(sstart + sb) + sdelta, sc.s_off);
+                        const uint32_t send = min(__ldg(sstart + sb + 1) + sdelta, sc.s_off + sc.s);
+                        for (uint32_t j = sbeg; j < send; ++j) {
+                            const float4 q = __ldg(spos + j);
+                            float dx = __fsub_rn(q.x, p.x), dy = __fsub_rn(q.y, p.y), dz = __fsub_rn(q.z, p.z);
+                            const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                            if (r2 <= h2) {
+                                const float r = __fsqrt_rn(r2);
+                                if (r < h) {
+                                    if (r2 == 0.f || r == 0.f) {
+                                        const float3 d = random_direction((float)__float_as_uint(p.w));
+                                        dx = d.x; dy = d.y; dz = d.z;
+                                    } else {
+                                        const float inv = __frcp_rn(r);
+                                        dx = __fmul_rn(dx, inv); dy = __fmul_rn(dy, inv); dz = __fmul_rn(dz, inv);
+                                    }
+                                    const float w = __fsub_rn(h, r);
+                                    const float pp = __fmul_rn(api, __fmul_rn(__fmul_rn(-3.f, w), w));
+                                    fs.x = __fmaf_rn(dx, pp, fs.x);
+                                    fs.y = __fmaf_rn(dy, pp, fs.y);
+                                    fs.z = __fmaf_rn(dz, pp, fs.z);
+                                }
+                            }
+                        }
+                    }
+                }
+        // SF:626-642 in the reference's operation order, without contraction
+        const float s1 = __fmul_rn(__fdiv_rn(sc.mass, __fmul_rn(2.f, rho)), sc.kc);
+        const float s2 = __fmul_rn(__fmul_rn(sc.visc, sc.mass), sc.kc);
+        float3 f;
+        f.x = __fadd_rn(__fadd_rn(__fmul_rn(fp.x, s1), __fmul_rn(fv.x, s2)), __fmul_rn(fs.x, s1));
+        f.y = __fadd_rn(__fadd_rn(__fmul_rn(fp.y, s1), __fmul_rn(fv.y, s2)), __fmul_rn(fs.y, s1));
+        f.z = __fadd_rn(__fadd_rn(__fmul_rn(fp.z, s1), __fmul_rn(fv.z, s2)), __fmul_rn(fs.z, s1));
+        for (uint32_t t = 0; t < sc.t; ++t) {
+            const float3 tf = triangle_force(make_float3(p.x, p.y, p.z), tris + 9u * (sc.t_off + t));
+            f.x = __fadd_rn(f.x, tf.x); f.y = __fadd_rn(f.y, tf.y); f.z = __fadd_rn(f.z, tf.z);
+        }
+        float3 acc;
+        acc.x = __fadd_rn(__fdiv_rn(f.x, rho), sc.gx);
+        acc.y = __fadd_rn(__fdiv_rn(f.y, rho), sc.gy);
+        acc.z = __fadd_rn(__fdiv_rn(f.z, rho), sc.gz);
+        float3 nv, np;
+        nv.x = __fadd_rn(v.x, __fmul_rn(acc.x, sc.dt));
+        nv.y = __fadd_rn(v.y, __fmul_rn(acc.y, sc.dt));
+        nv.z = __fadd_rn(v.z, __fmul_rn(acc.z, sc.dt));
+        np.x = __fadd_rn(p.x, __fmul_rn(nv.x, sc.dt));
+        np.y = __fadd_rn(p.y, __fmul_rn(nv.y, sc.dt));
+        np.z = __fadd_rn(p.z, __fmul_rn(nv.z, sc.dt));
+        k = fast_mod(cell_hash(np.x, np.y, np.z, h), sc.fm_b);
+        g = sc.q_off + k;
+        pos_out[i] = make_float4(np.x, np.y, np.z, p.w);
+        vel_out[i] = make_float4(nv.x, nv.y, nv.z, pi);
+        key_out[i] = k;
+        if (kRecordAccel) accel[i] = make_float4(acc.x, acc.y, acc.z, 0.f);
+    }
+    const uint32_t r = warp_aggregated_increment(count, g, valid);
+    if (valid) arrival[i] = r;
+}
+
+}  // namespace sph

@@ -1,0 +1,121 @@
+// sph_state.h -- device state of one or more SPH scenes and the launches
+// that advance it.  Used by the single-scene engine, the batch and the
+// server behind the C ABI in include/sph_gb300.h.
+#pragma once
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "sph_gb300.h"
+#include "sph_kernels.cuh"
+
+namespace sph {
+
+constexpr uint64_t kMaxParticles = 1ull << 30;
+
+struct SortArgs {
+    const Tile* tiles;
+    const SceneDesc* scenes;
+    const float4* pos_src;
+    const float4* vel_src;
+    float4* pos_dst;
+    float4* vel_dst;
+    uint32_t* key;
+    uint32_t* arrival;
+    uint32_t* perm;
+    uint32_t* count;
+    uint32_t* start;
+    uint32_t* err;
+};
+
+// One scene as the caller hands it over (host pointers, caller's order).
+struct SceneInput {
+    sph_params params{};
+    const float* pos = nullptr;    // n x 3
+    const float* vel = nullptr;    // n x 3 or null
+    uint32_t n = 0;
+    const float* spos = nullptr;   // s x 3
+    uint32_t s = 0;
+    const float* tris = nullptr;   // t x 9
+    uint32_t t = 0;
+    float dt = 0.f;
+    uint32_t buckets = 0;          // dynamic bucket count; 0 = 2n (SimulationEngineCPU.cpp:486)
+};
+
+enum class StepMode { Staged = 0, Persistent = 1 };
+
+void set_last_error(const std::string& s);
+const char* last_error();
+sph_status validate_scene(const SceneInput& in);
+
+class StepState {
+public:
+    StepState() = default;
+    StepState(const StepState&) = delete;
+    StepState& operator=(const StepState&) = delete;
+    ~StepState();
+
+    // Lays the scenes out back to back, allocates, uploads and sorts them.
+    sph_status build(int device, cudaStream_t stream, const std::vector<SceneInput>& inputs);
+    void release();
+
+    // Queues `steps` steps of every scene.  Staged mode replays a captured
+    // CUDA graph of the five stage launches; persistent mode issues one
+    // cooperative launch per step.  `timed` records per-stage events.
+    sph_status enqueue_steps(uint32_t steps, StepMode mode, bool record_accel, bool timed);
+    sph_status check_device_error();
+
+    sph_status set_dt(uint32_t scene, float dt);
+    sph_status read_scene(uint32_t scene, sph_dynamic_particle* out, float* accel_out);
+    sph_status write_scene(uint32_t scene, const sph_dynamic_particle* in);
+    sph_status read_static(uint32_t scene, sph_static_particle* out, uint32_t* bucket_starts);
+    sph_status read_buckets(uint32_t scene, uint32_t* bucket_starts, uint32_t* slot_ids);
+    sph_status persistent_grid(uint32_t* grid);
+    // Outputs of the initial sort of scene 0 (see sph_cell_sort).
+    sph_status read_sort(uint32_t* keys, uint32_t* counts, uint32_t* starts, uint32_t* order);
+
+    const float* stage_ms() const { return stage_ms_; }
+    void set_persistent_ctas(uint32_t c) { persistent_ctas_ = c; }
+
+    std::vector<SceneDesc> scenes;
+    std::vector<Tile> tiles, stiles;
+    uint32_t total_n = 0, total_s = 0, total_t = 0;
+    uint32_t scan_len = 0, sscan_len = 0;
+
+    // device arrays
+    SceneDesc* d_scenes = nullptr;
+    SceneDesc* d_sscenes = nullptr;
+    Tile* d_tiles = nullptr;
+    Tile* d_stiles = nullptr;
+    float4 *pos = nullptr, *vel = nullptr, *pos_tmp = nullptr, *vel_tmp = nullptr;
+    uint32_t *key = nullptr, *arrival = nullptr, *perm = nullptr, *count = nullptr, *start = nullptr;
+    unsigned long long* scan_status = nullptr;
+    uint32_t* scan_ticket = nullptr;
+    uint32_t* err = nullptr;
+    uint32_t* bar = nullptr;
+    float4* spos = nullptr;
+    uint32_t* sstart = nullptr;
+    float* tris = nullptr;
+    float4* accel = nullptr;
+    float4* accel_io = nullptr;
+    float4* staging = nullptr;
+
+private:
+    sph_status enqueue_load(const float4* src, bool statics);
+    sph_status enqueue_sort(bool statics);
+    sph_status enqueue_scan(uint32_t* out, uint32_t len);
+    sph_status enqueue_step_staged(bool record_accel, bool timed);
+    sph_status enqueue_step_persistent();
+    sph_status ensure_events();
+    SortArgs sort_args(bool statics) const;
+    StepArgs step_args() const;
+
+    int device_ = 0;
+    cudaStream_t stream_ = nullptr;
+    cudaGraphExec_t graph_ = nullptr;
+    cudaEvent_t events_[6] = {};
+    float stage_ms_[5] = {};
+    uint32_t persistent_ctas_ = 0;
+};
+
+}  // namespace sph

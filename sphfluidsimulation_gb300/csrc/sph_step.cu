@@ -1,0 +1,722 @@
+// sph_step.cu -- kernels of the SPH step and the device-state object that
+// launches them (one scene or many).
+//
+// Per step, over every tile of every scene:
+//   density  (vel.w = pressure)                      reference SF:358-501
+//   force    (tmp = integrated particles, key, count) reference SF:503-656
+//   scan     (start = exclusive scan of count)        reference SF:227-294 / ECPU:245-253
+//   scatter  (perm[start+arrival] = tmp slot)         reference SF:346-356
+//   gather   (stable rank, tmp -> sorted state)       reference SF:332-345
+// either as five launches (captured once in a CUDA graph) or as one
+// persistent cooperative launch with four bounded grid barriers.
+#include "sph_state.h"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+
+namespace sph {
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kTileThreads) k_hash_count(SortArgs a)
+{
+    hash_count_tile(a.tiles[blockIdx.x], a.scenes, a.pos_src, a.key, a.arrival, a.count);
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan(uint32_t* count, uint32_t* start, uint32_t len,
+                                                       unsigned long long* status, uint32_t* ticket, uint32_t* err)
+{
+    __shared__ ScanSmem sm;
+    if (threadIdx.x == 0) sm.tile = atomicAdd(ticket, 1u);
+    __syncthreads();
+    scan_tile(sm.tile, count, start, len, status, err, sm);
+}
+
+__global__ void __launch_bounds__(kTileThreads) k_scatter(SortArgs a)
+{
+    scatter_tile(a.tiles[blockIdx.x], a.scenes, a.key, a.arrival, a.start, a.perm, a.err);
+}
+
+__global__ void __launch_bounds__(kTileThreads) k_gather(SortArgs a)
+{
+    gather_tile(a.tiles[blockIdx.x], a.scenes, a.key, a.arrival, a.perm, a.start, a.pos_src, a.vel_src,
+                a.pos_dst, a.vel_dst, a.err);
+}
+
+__global__ void __launch_bounds__(kTileThreads) k_density(StepArgs a)
+{
+    density_tile(a.tiles[blockIdx.x], a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart);
+}
+
+template <bool kRecord>
+__global__ void __launch_bounds__(kTileThreads) k_force(StepArgs a)
+{
+    force_tile<kRecord>(a.tiles[blockIdx.x], a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart, a.tris,
+                        a.pos_tmp, a.vel_tmp, a.key, a.arrival, a.count, a.accel);
+}
+
+// Bounded grid barrier for the persistent kernel (all CTAs co-resident by
+// cooperative launch).  Sense by generation counter; on expiry the error word
+// is set and the CTA proceeds, so the launch always terminates.
+__device__ __forceinline__ void grid_barrier(uint32_t* count, uint32_t* gen, uint32_t* err)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t g0 = *(volatile uint32_t*)gen;
+        __threadfence();
+        if (atomicAdd(count, 1u) == gridDim.x - 1u) {
+            atomicExch(count, 0u);
+            __threadfence();
+            atomicAdd(gen, 1u);
+        } else {
+            uint32_t spins = 0;
+            while (*(volatile uint32_t*)gen == g0) {
+                if (++spins > kSpinLimit) { atomicOr(err, DEV_ERR_BARRIER_TIMEOUT); break; }
+                __nanosleep(spins < 64 ? 32 : 256);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+// One whole step in one launch: density, force, scan, scatter, gather with a
+// grid barrier between stages.  Tiles are taken grid-stride; scan tiles are
+// taken in increasing order per CTA, so every look-back waits only on a tile
+// a co-resident CTA reaches first.
+__global__ void __launch_bounds__(kTileThreads) k_step_persistent(StepArgs a, uint32_t scan_tiles)
+{
+    __shared__ ScanSmem sm;
+    // the previous scan (any launch before this one) is complete: clear its
+    // tile status so this step's look-back starts from empty
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < scan_tiles; t += gridDim.x * blockDim.x)
+        a.scan_status[t] = 0ull;
+    for (uint32_t t = blockIdx.x; t < a.num_tiles; t += gridDim.x)
+        density_tile(a.tiles[t], a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart);
+    grid_barrier(a.bar_count, a.bar_gen, a.err);
+    for (uint32_t t = blockIdx.x; t < a.num_tiles; t += gridDim.x)
+        force_tile<false>(a.tiles[t], a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart, a.tris, a.pos_tmp,
+                          a.vel_tmp, a.key, a.arrival, a.count, a.accel);
+    grid_barrier(a.bar_count, a.bar_gen, a.err);
+    for (uint32_t t = blockIdx.x; t < scan_tiles; t += gridDim.x)
+        scan_tile(t, a.count, a.start, a.scan_len, a.scan_status, a.err, sm);
+    grid_barrier(a.bar_count, a.bar_gen, a.err);
+    for (uint32_t t = blockIdx.x; t < a.num_tiles; t += gridDim.x)
+        scatter_tile(a.tiles[t], a.scenes, a.key, a.arrival, a.start, a.perm, a.err);
+    grid_barrier(a.bar_count, a.bar_gen, a.err);
+    for (uint32_t t = blockIdx.x; t < a.num_tiles; t += gridDim.x)
+        gather_tile(a.tiles[t], a.scenes, a.key, a.arrival, a.perm, a.start, a.pos_tmp, a.vel_tmp, a.pos, a.vel,
+                    a.err);
+}
+
+// Readback: sorted slot i -> caller's order, in the reference's 32-byte layout
+// (Particles.h:9-17); hash = key of the position (SF:644-645).
+__global__ void __launch_bounds__(kTileThreads) k_unsort(const Tile* tiles, const SceneDesc* scenes, const float4* pos,
+                                                         const float4* vel, float4* out, const float4* accel_in,
+                                                         float4* accel_out)
+{
+    const Tile tile = tiles[blockIdx.x];
+    const SceneDesc& sc = scenes[tile.scene];
+    const uint32_t i = tile.begin + threadIdx.x;
+    if (i >= tile.end) return;
+    const float4 p = pos[i];
+    const float4 v = vel[i];
+    const uint32_t id = __float_as_uint(p.w);
+    if (id >= sc.n) return;
+    const uint32_t key = fast_mod(cell_hash(p.x, p.y, p.z, sc.h), sc.fm_b);
+    const uint32_t o = sc.p_off + id;
+    out[2 * (size_t)o] = make_float4(p.x, p.y, p.z, v.w);
+    out[2 * (size_t)o + 1] = make_float4(v.x, v.y, v.z, __uint_as_float(key));
+    if (accel_in) accel_out[o] = accel_in[i];
+}
+
+// Upload staging (caller's order, positions and velocities as float4 pairs)
+// -> unsorted tmp arrays with the input index in pos.w.
+__global__ void __launch_bounds__(kTileThreads) k_load(const Tile* tiles, const SceneDesc* scenes, const float4* in,
+                                                       float4* pos_tmp, float4* vel_tmp)
+{
+    const Tile tile = tiles[blockIdx.x];
+    const SceneDesc& sc = scenes[tile.scene];
+    const uint32_t i = tile.begin + threadIdx.x;
+    if (i >= tile.end) return;
+    const float4 p = in[2 * (size_t)i];
+    const float4 v = in[2 * (size_t)i + 1];
+    pos_tmp[i] = make_float4(p.x, p.y, p.z, __uint_as_float(i - sc.p_off));
+    vel_tmp[i] = make_float4(v.x, v.y, v.z, 0.f);
+}
+
+// ---------------------------------------------------------------------------
+// StepState host side
+// ---------------------------------------------------------------------------
+
+thread_local std::string g_last_error;
+
+void set_last_error(const std::string& s) { g_last_error = s; }
+const char* last_error() { return g_last_error.c_str(); }
+
+#define CUDA_TRY(expr)                                                                              \
+    do {                                                                                            \
+        cudaError_t e_ = (expr);                                                                    \
+        if (e_ != cudaSuccess) {                                                                    \
+            set_last_error(std::string(#expr) + ": " + cudaGetErrorString(e_));                    \
+            return e_ == cudaErrorMemoryAllocation ? SPH_ERR_OUT_OF_MEMORY : SPH_ERR_CUDA;          \
+        }                                                                                           \
+    } while (0)
+
+template <typename T>
+static sph_status dev_alloc(T** p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0) count = 1;
+    CUDA_TRY(cudaMalloc((void**)p, sizeof(T) * count));
+    return SPH_OK;
+}
+
+StepState::~StepState() { release(); }
+
+void StepState::release()
+{
+    if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+    void* ptrs[] = {d_scenes, d_sscenes, d_tiles, d_stiles, pos, vel, pos_tmp, vel_tmp, key, arrival, perm, count,
+                    start, scan_status, scan_ticket, err, bar, spos, sstart, tris, accel, accel_io, staging};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    d_scenes = d_sscenes = nullptr;
+    d_tiles = d_stiles = nullptr;
+    pos = vel = pos_tmp = vel_tmp = spos = accel = accel_io = nullptr;
+    staging = nullptr;
+    key = arrival = perm = count = start = scan_ticket = err = bar = sstart = nullptr;
+    scan_status = nullptr;
+    tris = nullptr;
+    for (auto& e : events_)
+        if (e) cudaEventDestroy(e);
+    for (auto& e : events_) e = nullptr;
+    scenes.clear();
+    tiles.clear();
+    stiles.clear();
+    total_n = total_s = total_t = 0;
+    scan_len = sscan_len = 0;
+}
+
+static SceneDesc make_scene_desc(const sph_params& p, float dt)
+{
+    SceneDesc d{};
+    d.h = p.max_interaction_distance;
+    d.h2 = d.h * d.h;
+    d.mass = p.particle_mass;
+    d.gas = p.gas_constant;
+    d.rho0 = p.rest_density;
+    d.visc = p.viscosity;
+    d.gx = p.gravity_x;
+    d.gy = p.gravity_y;
+    d.gz = p.gravity_z;
+    d.kc = kernel_constant(d.h);
+    d.self_density = self_density(d.mass, d.h, d.kc);
+    d.dt = dt;
+    return d;
+}
+
+sph_status validate_scene(const SceneInput& in)
+{
+    const sph_params& p = in.params;
+    if (!(p.max_interaction_distance > 0.f) || !std::isfinite(p.max_interaction_distance)) {
+        set_last_error("max_interaction_distance must be a positive finite number");
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    if (!(p.gas_constant != 0.f)) {
+        set_last_error("gas_constant must be non-zero (the force pass divides by it)");
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    if (in.n && !in.pos) { set_last_error("dyn_pos is null"); return SPH_ERR_INVALID_ARGUMENT; }
+    if (in.s && !in.spos) { set_last_error("static_pos is null"); return SPH_ERR_INVALID_ARGUMENT; }
+    if (in.t && !in.tris) { set_last_error("triangles is null"); return SPH_ERR_INVALID_ARGUMENT; }
+    if (in.n > kMaxParticles || in.s > kMaxParticles) {
+        set_last_error("particle count exceeds 2^30");
+        return SPH_ERR_CAPACITY;
+    }
+    return SPH_OK;
+}
+
+sph_status StepState::build(int device, cudaStream_t stream, const std::vector<SceneInput>& inputs)
+{
+    release();
+    device_ = device;
+    stream_ = stream;
+    uint64_t p_off = 0, q_off = 0, s_off = 0, sq_off = 0, t_off = 0;
+    for (size_t k = 0; k < inputs.size(); ++k) {
+        const SceneInput& in = inputs[k];
+        sph_status st = validate_scene(in);
+        if (st != SPH_OK) return st;
+        SceneDesc d = make_scene_desc(in.params, in.dt);
+        d.p_off = (uint32_t)p_off;
+        d.n = in.n;
+        d.q_off = (uint32_t)q_off;
+        d.buckets = in.buckets ? in.buckets : 2u * in.n;
+        d.s_off = (uint32_t)s_off;
+        d.s = in.s;
+        d.sq_off = (uint32_t)sq_off;
+        d.t_off = (uint32_t)t_off;
+        d.t = in.t;
+        d.fm_b = make_fastmod(d.buckets);
+        d.fm_s = make_fastmod(in.s);
+        scenes.push_back(d);
+        for (uint32_t b = 0; b < in.n; b += kTileThreads)
+            tiles.push_back(Tile{(uint32_t)k, (uint32_t)(p_off + b), (uint32_t)(p_off + std::min<uint64_t>(b + kTileThreads, in.n)), 0});
+        for (uint32_t b = 0; b < in.s; b += kTileThreads)
+            stiles.push_back(Tile{(uint32_t)k, (uint32_t)(s_off + b), (uint32_t)(s_off + std::min<uint64_t>(b + kTileThreads, in.s)), 0});
+        p_off += in.n;
+        q_off += d.buckets;
+        s_off += in.s;
+        sq_off += in.s;
+        t_off += in.t;
+    }
+    if (p_off > kMaxParticles || s_off > kMaxParticles || q_off >= (1ull << 31)) {
+        set_last_error("total particle count exceeds 2^30");
+        return SPH_ERR_CAPACITY;
+    }
+    total_n = (uint32_t)p_off;
+    total_s = (uint32_t)s_off;
+    total_t = (uint32_t)t_off;
+    scan_len = (uint32_t)q_off + 1u;
+    sscan_len = (uint32_t)sq_off + 1u;
+    const uint32_t scan_tiles_max = (std::max(scan_len, sscan_len) + kScanTile - 1) / kScanTile;
+    const uint32_t work_n = std::max(total_n, total_s);
+
+    sph_status st;
+#define ALLOC(ptr, cnt) if ((st = dev_alloc(&(ptr), (cnt))) != SPH_OK) return st
+    ALLOC(d_scenes, scenes.size());
+    ALLOC(d_sscenes, scenes.size());
+    ALLOC(d_tiles, tiles.size());
+    ALLOC(d_stiles, stiles.size());
+    ALLOC(pos, total_n);
+    ALLOC(vel, total_n);
+    ALLOC(pos_tmp, work_n);
+    ALLOC(vel_tmp, work_n);
+    ALLOC(key, work_n);
+    ALLOC(arrival, work_n);
+    ALLOC(perm, work_n);
+    ALLOC(count, std::max(scan_len, sscan_len));
+    ALLOC(start, scan_len);
+    ALLOC(scan_status, scan_tiles_max);
+    ALLOC(scan_ticket, 1);
+    ALLOC(err, 1);
+    ALLOC(bar, 2);
+    ALLOC(spos, total_s);
+    ALLOC(sstart, sscan_len);
+    ALLOC(tris, 9ull * total_t);
+    ALLOC(staging, 2ull * std::max(total_n, total_s));
+#undef ALLOC
+    CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(uint32_t) * std::max(scan_len, sscan_len), stream_));
+    CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(uint32_t), stream_));
+    CUDA_TRY(cudaMemsetAsync(bar, 0, 2 * sizeof(uint32_t), stream_));
+    CUDA_TRY(cudaMemsetAsync(scan_status, 0, sizeof(unsigned long long) * scan_tiles_max, stream_));
+    CUDA_TRY(cudaMemcpyAsync(d_scenes, scenes.data(), sizeof(SceneDesc) * scenes.size(), cudaMemcpyHostToDevice, stream_));
+    // static view: the same scenes with the static index spaces in the
+    // dynamic fields, so the sort kernels serve both particle kinds
+    std::vector<SceneDesc> sview = scenes;
+    for (auto& d : sview) {
+        d.p_off = d.s_off;
+        d.n = d.s;
+        d.q_off = d.sq_off;
+        d.buckets = d.s;
+        d.fm_b = d.fm_s;
+    }
+    CUDA_TRY(cudaMemcpyAsync(d_sscenes, sview.data(), sizeof(SceneDesc) * sview.size(), cudaMemcpyHostToDevice, stream_));
+    if (!tiles.empty())
+        CUDA_TRY(cudaMemcpyAsync(d_tiles, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice, stream_));
+    if (!stiles.empty())
+        CUDA_TRY(cudaMemcpyAsync(d_stiles, stiles.data(), sizeof(Tile) * stiles.size(), cudaMemcpyHostToDevice, stream_));
+    CUDA_TRY(cudaStreamSynchronize(stream_));
+
+    // upload every scene, then sort statics and dynamics
+    std::vector<float> hbuf;
+    for (size_t k = 0; k < inputs.size(); ++k) {
+        const SceneInput& in = inputs[k];
+        const SceneDesc& d = scenes[k];
+        if (in.s) {
+            hbuf.assign(8ull * in.s, 0.f);
+            for (uint32_t i = 0; i < in.s; ++i) {
+                hbuf[8ull * i + 0] = in.spos[3ull * i + 0];
+                hbuf[8ull * i + 1] = in.spos[3ull * i + 1];
+                hbuf[8ull * i + 2] = in.spos[3ull * i + 2];
+            }
+            CUDA_TRY(cudaMemcpyAsync(staging + 2ull * d.s_off, hbuf.data(), sizeof(float) * hbuf.size(), cudaMemcpyHostToDevice, stream_));
+            CUDA_TRY(cudaStreamSynchronize(stream_));
+        }
+        if (in.t)
+            CUDA_TRY(cudaMemcpyAsync(tris + 9ull * d.t_off, in.tris, sizeof(float) * 9ull * in.t, cudaMemcpyHostToDevice, stream_));
+    }
+    if (total_s) {
+        if ((st = enqueue_load(staging, /*statics=*/true)) != SPH_OK) return st;
+        if ((st = enqueue_sort(/*statics=*/true)) != SPH_OK) return st;
+    }
+    for (size_t k = 0; k < inputs.size(); ++k) {
+        const SceneInput& in = inputs[k];
+        const SceneDesc& d = scenes[k];
+        if (!in.n) continue;
+        hbuf.assign(8ull * in.n, 0.f);
+        for (uint32_t i = 0; i < in.n; ++i) {
+            hbuf[8ull * i + 0] = in.pos[3ull * i + 0];
+            hbuf[8ull * i + 1] = in.pos[3ull * i + 1];
+            hbuf[8ull * i + 2] = in.pos[3ull * i + 2];
+            if (in.vel) {
+                hbuf[8ull * i + 4] = in.vel[3ull * i + 0];
+                hbuf[8ull * i + 5] = in.vel[3ull * i + 1];
+                hbuf[8ull * i + 6] = in.vel[3ull * i + 2];
+            }
+        }
+        CUDA_TRY(cudaMemcpyAsync(staging + 2ull * d.p_off, hbuf.data(), sizeof(float) * hbuf.size(), cudaMemcpyHostToDevice, stream_));
+        CUDA_TRY(cudaStreamSynchronize(stream_));
+    }
+    if (total_n) {
+        if ((st = enqueue_load(staging, false)) != SPH_OK) return st;
+        if ((st = enqueue_sort(false)) != SPH_OK) return st;
+    }
+    CUDA_TRY(cudaStreamSynchronize(stream_));
+    return check_device_error();
+}
+
+sph_status StepState::enqueue_load(const float4* src, bool statics)
+{
+    const std::vector<Tile>& tl = statics ? stiles : tiles;
+    if (tl.empty()) return SPH_OK;
+    k_load<<<(unsigned)tl.size(), kTileThreads, 0, stream_>>>(statics ? d_stiles : d_tiles, statics ? d_sscenes : d_scenes,
+                                                                src, pos_tmp, vel_tmp);
+    CUDA_TRY(cudaGetLastError());
+    return SPH_OK;
+}
+
+SortArgs StepState::sort_args(bool statics) const
+{
+    SortArgs a{};
+    a.tiles = statics ? d_stiles : d_tiles;
+    a.scenes = statics ? d_sscenes : d_scenes;
+    a.pos_src = pos_tmp;
+    a.vel_src = vel_tmp;
+    a.pos_dst = statics ? spos : pos;
+    a.vel_dst = statics ? staging : vel;   // static velocities are discarded
+    a.key = key;
+    a.arrival = arrival;
+    a.perm = perm;
+    a.count = count;
+    a.start = statics ? sstart : start;
+    a.err = err;
+    return a;
+}
+
+// Counting sort of the tmp arrays into the sorted state: hash + count, scan,
+// scatter, stable gather (positions must already be in pos_tmp).
+sph_status StepState::enqueue_sort(bool statics)
+{
+    const std::vector<Tile>& tl = statics ? stiles : tiles;
+    if (tl.empty()) return SPH_OK;
+    SortArgs a = sort_args(statics);
+    const uint32_t len = statics ? sscan_len : scan_len;
+    const unsigned nt = (unsigned)tl.size();
+    k_hash_count<<<nt, kTileThreads, 0, stream_>>>(a);
+    CUDA_TRY(cudaGetLastError());
+    sph_status st = enqueue_scan(a.start, len);
+    if (st != SPH_OK) return st;
+    k_scatter<<<nt, kTileThreads, 0, stream_>>>(a);
+    CUDA_TRY(cudaGetLastError());
+    k_gather<<<nt, kTileThreads, 0, stream_>>>(a);
+    CUDA_TRY(cudaGetLastError());
+    return SPH_OK;
+}
+
+sph_status StepState::enqueue_scan(uint32_t* out, uint32_t len)
+{
+    const uint32_t tiles_n = (len + kScanTile - 1) / kScanTile;
+    CUDA_TRY(cudaMemsetAsync(scan_status, 0, sizeof(unsigned long long) * tiles_n, stream_));
+    CUDA_TRY(cudaMemsetAsync(scan_ticket, 0, sizeof(uint32_t), stream_));
+    k_scan<<<tiles_n, kScanThreads, 0, stream_>>>(count, out, len, scan_status, scan_ticket, err);
+    CUDA_TRY(cudaGetLastError());
+    return SPH_OK;
+}
+
+StepArgs StepState::step_args() const
+{
+    StepArgs a{};
+    a.tiles = d_tiles;
+    a.num_tiles = (uint32_t)tiles.size();
+    a.scenes = d_scenes;
+    a.pos = pos;
+    a.vel = vel;
+    a.pos_tmp = pos_tmp;
+    a.vel_tmp = vel_tmp;
+    a.key = key;
+    a.arrival = arrival;
+    a.perm = perm;
+    a.count = count;
+    a.start = start;
+    a.scan_len = scan_len;
+    a.scan_status = scan_status;
+    a.scan_ticket = scan_ticket;
+    a.spos = spos;
+    a.sstart = sstart;
+    a.tris = tris;
+    a.accel = accel;
+    a.err = err;
+    a.bar_count = bar;
+    a.bar_gen = bar + 1;
+    return a;
+}
+
+sph_status StepState::ensure_events()
+{
+    for (auto& e : events_)
+        if (!e) CUDA_TRY(cudaEventCreate(&e));
+    return SPH_OK;
+}
+
+// One step as five launches (plus the scan's two memsets).  With `timed`,
+// events bracket each stage on the launching stream.
+sph_status StepState::enqueue_step_staged(bool record_accel, bool timed)
+{
+    if (tiles.empty()) return SPH_OK;
+    const unsigned nt = (unsigned)tiles.size();
+    StepArgs a = step_args();
+    SortArgs s = sort_args(false);
+    if (timed) CUDA_TRY(cudaEventRecord(events_[0], stream_));
+    k_density<<<nt, kTileThreads, 0, stream_>>>(a);
+    CUDA_TRY(cudaGetLastError());
+    if (timed) CUDA_TRY(cudaEventRecord(events_[1], stream_));
+    if (record_accel)
+        k_force<true><<<nt, kTileThreads, 0, stream_>>>(a);
+    else
+        k_force<false><<<nt, kTileThreads, 0, stream_>>>(a);
+    CUDA_TRY(cudaGetLastError());
+    if (timed) CUDA_TRY(cudaEventRecord(events_[2], stream_));
+    sph_status st = enqueue_scan(start, scan_len);
+    if (st != SPH_OK) return st;
+    if (timed) CUDA_TRY(cudaEventRecord(events_[3], stream_));
+    k_scatter<<<nt, kTileThreads, 0, stream_>>>(s);
+    CUDA_TRY(cudaGetLastError());
+    if (timed) CUDA_TRY(cudaEventRecord(events_[4], stream_));
+    k_gather<<<nt, kTileThreads, 0, stream_>>>(s);
+    CUDA_TRY(cudaGetLastError());
+    if (timed) CUDA_TRY(cudaEventRecord(events_[5], stream_));
+    return SPH_OK;
+}
+
+sph_status StepState::persistent_grid(uint32_t* grid)
+{
+    int sms = 0, per_sm = 0;
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step_persistent, kTileThreads, 0));
+    if (per_sm < 1) per_sm = 1;
+    uint32_t g = (uint32_t)(sms * per_sm);
+    if (persistent_ctas_ && persistent_ctas_ < g) g = persistent_ctas_;
+    *grid = std::max<uint32_t>(1, g);
+    return SPH_OK;
+}
+
+sph_status StepState::enqueue_step_persistent()
+{
+    if (tiles.empty()) return SPH_OK;
+    uint32_t grid = 0;
+    sph_status st = persistent_grid(&grid);
+    if (st != SPH_OK) return st;
+    StepArgs a = step_args();
+    uint32_t scan_tiles = (scan_len + kScanTile - 1) / kScanTile;
+    void* args[] = {&a, &scan_tiles};
+    CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_step_persistent, dim3(grid), dim3(kTileThreads), args, 0, stream_));
+    return SPH_OK;
+}
+
+// Captures one staged step into a graph (once per layout) and replays it.
+sph_status StepState::enqueue_steps(uint32_t steps, StepMode mode, bool record_accel, bool timed)
+{
+    if (tiles.empty() || steps == 0) return SPH_OK;
+    if (record_accel && !accel) {
+        sph_status st = dev_alloc(&accel, total_n);
+        if (st != SPH_OK) return st;
+        if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+    }
+    if (timed) {
+        sph_status st = ensure_events();
+        if (st != SPH_OK) return st;
+        for (float& t : stage_ms_) t = 0.f;
+        for (uint32_t k = 0; k < steps; ++k) {
+            st = (mode == StepMode::Persistent) ? enqueue_step_persistent() : enqueue_step_staged(record_accel, true);
+            if (st != SPH_OK) return st;
+            if (mode != StepMode::Persistent) {
+                CUDA_TRY(cudaEventSynchronize(events_[5]));
+                for (int s = 0; s < 5; ++s) {
+                    float ms = 0.f;
+                    CUDA_TRY(cudaEventElapsedTime(&ms, events_[s], events_[s + 1]));
+                    stage_ms_[s] += ms;
+                }
+            }
+        }
+        return SPH_OK;
+    }
+    if (mode == StepMode::Persistent) {
+        for (uint32_t k = 0; k < steps; ++k) {
+            sph_status st = enqueue_step_persistent();
+            if (st != SPH_OK) return st;
+        }
+        return SPH_OK;
+    }
+    if (record_accel) {
+        for (uint32_t k = 0; k < steps; ++k) {
+            sph_status st = enqueue_step_staged(true, false);
+            if (st != SPH_OK) return st;
+        }
+        return SPH_OK;
+    }
+    if (!graph_) {
+        cudaGraph_t g = nullptr;
+        CUDA_TRY(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+        sph_status st = enqueue_step_staged(false, false);
+        cudaError_t e = cudaStreamEndCapture(stream_, &g);
+        if (st != SPH_OK) { if (g) cudaGraphDestroy(g); return st; }
+        if (e != cudaSuccess) { set_last_error(std::string("graph capture: ") + cudaGetErrorString(e)); return SPH_ERR_CUDA; }
+        e = cudaGraphInstantiate(&graph_, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) { graph_ = nullptr; set_last_error(std::string("graph instantiate: ") + cudaGetErrorString(e)); return SPH_ERR_CUDA; }
+    }
+    for (uint32_t k = 0; k < steps; ++k) CUDA_TRY(cudaGraphLaunch(graph_, stream_));
+    return SPH_OK;
+}
+
+sph_status StepState::check_device_error()
+{
+    if (!err) return SPH_OK;
+    uint32_t h = 0;
+    CUDA_TRY(cudaMemcpyAsync(&h, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
+    CUDA_TRY(cudaStreamSynchronize(stream_));
+    if (h) {
+        CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(uint32_t), stream_));
+        CUDA_TRY(cudaMemsetAsync(bar, 0, 2 * sizeof(uint32_t), stream_));
+        char msg[160];
+        snprintf(msg, sizeof msg, "device status 0x%x (1 scan wait, 2 barrier wait, 4 slot range, 8 bucket range)", h);
+        set_last_error(msg);
+        return (h & (DEV_ERR_SCAN_TIMEOUT | DEV_ERR_BARRIER_TIMEOUT)) ? SPH_ERR_DEVICE_TIMEOUT : SPH_ERR_CUDA;
+    }
+    return SPH_OK;
+}
+
+sph_status StepState::set_dt(uint32_t scene, float dt)
+{
+    if (scene >= scenes.size()) return SPH_ERR_NOT_FOUND;
+    if (scenes[scene].dt == dt) return SPH_OK;
+    scenes[scene].dt = dt;
+    CUDA_TRY(cudaMemcpyAsync(&d_scenes[scene].dt, &scenes[scene].dt, sizeof(float), cudaMemcpyHostToDevice, stream_));
+    CUDA_TRY(cudaStreamSynchronize(stream_));
+    return SPH_OK;
+}
+
+// Reads one scene's particles (caller's order) into host `out` (n x 32 B).
+sph_status StepState::read_scene(uint32_t scene, sph_dynamic_particle* out, float* accel_out)
+{
+    if (scene >= scenes.size()) return SPH_ERR_NOT_FOUND;
+    const SceneDesc& d = scenes[scene];
+    if (!d.n) return SPH_OK;
+    if (accel_out && !accel) { set_last_error("acceleration recording is off"); return SPH_ERR_INVALID_ARGUMENT; }
+    if (accel_out && !accel_io) {
+        sph_status st = dev_alloc(&accel_io, total_n);
+        if (st != SPH_OK) return st;
+    }
+    k_unsort<<<(unsigned)tiles.size(), kTileThreads, 0, stream_>>>(d_tiles, d_scenes, pos, vel, staging,
+                                                                  accel_out ? accel : nullptr, accel_io);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(out, staging + 2ull * d.p_off, sizeof(sph_dynamic_particle) * d.n, cudaMemcpyDeviceToHost, stream_));
+    if (accel_out) {
+        std::vector<float4> tmp(d.n);
+        CUDA_TRY(cudaMemcpyAsync(tmp.data(), accel_io + d.p_off, sizeof(float4) * d.n, cudaMemcpyDeviceToHost, stream_));
+        CUDA_TRY(cudaStreamSynchronize(stream_));
+        for (uint32_t i = 0; i < d.n; ++i) {
+            accel_out[3ull * i + 0] = tmp[i].x;
+            accel_out[3ull * i + 1] = tmp[i].y;
+            accel_out[3ull * i + 2] = tmp[i].z;
+        }
+    }
+    CUDA_TRY(cudaStreamSynchronize(stream_));
+    return check_device_error();
+}
+
+// Replaces one scene's particles from host (caller's order) and re-sorts the
+// whole state (other scenes are re-sorted unchanged).
+sph_status StepState::write_scene(uint32_t scene, const sph_dynamic_particle* in)
+{
+    if (scene >= scenes.size()) return SPH_ERR_NOT_FOUND;
+    const SceneDesc& d = scenes[scene];
+    if (!d.n) return SPH_OK;
+    // move the current sorted state of all scenes into staging order first
+    k_unsort<<<(unsigned)tiles.size(), kTileThreads, 0, stream_>>>(d_tiles, d_scenes, pos, vel, staging, nullptr, nullptr);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(staging + 2ull * d.p_off, in, sizeof(sph_dynamic_particle) * d.n, cudaMemcpyHostToDevice, stream_));
+    sph_status st = enqueue_load(staging, false);
+    if (st != SPH_OK) return st;
+    st = enqueue_sort(false);
+    if (st != SPH_OK) return st;
+    CUDA_TRY(cudaStreamSynchronize(stream_));
+    return check_device_error();
+}
+
+sph_status StepState::read_static(uint32_t scene, sph_static_particle* out, uint32_t* bucket_starts)
+{
+    if (scene >= scenes.size()) return SPH_ERR_NOT_FOUND;
+    const SceneDesc& d = scenes[scene];
+    if (!d.s) return SPH_OK;
+    if (out) {
+        CUDA_TRY(cudaMemcpyAsync(out, spos + d.s_off, sizeof(float4) * d.s, cudaMemcpyDeviceToHost, stream_));
+    }
+    CUDA_TRY(cudaStreamSynchronize(stream_));
+    if (out) {
+        for (uint32_t i = 0; i < d.s; ++i) out[i].pressure = 0.f;   // static pressure is never written
+    }
+    if (bucket_starts) {
+        CUDA_TRY(cudaMemcpy(bucket_starts, sstart + d.sq_off, sizeof(uint32_t) * (d.s + 1ull), cudaMemcpyDeviceToHost));
+        const uint32_t b0 = bucket_starts[0];
+        for (uint32_t k = 0; k <= d.s; ++k) bucket_starts[k] -= b0;
+    }
+    return SPH_OK;
+}
+
+sph_status StepState::read_buckets(uint32_t scene, uint32_t* bucket_starts, uint32_t* slot_ids)
+{
+    if (scene >= scenes.size()) return SPH_ERR_NOT_FOUND;
+    const SceneDesc& d = scenes[scene];
+    if (!d.n) return SPH_OK;
+    CUDA_TRY(cudaStreamSynchronize(stream_));
+    if (bucket_starts) {
+        CUDA_TRY(cudaMemcpy(bucket_starts, start + d.q_off, sizeof(uint32_t) * (d.buckets + 1ull), cudaMemcpyDeviceToHost));
+        const uint32_t b0 = bucket_starts[0];
+        for (uint32_t k = 0; k <= d.buckets; ++k) bucket_starts[k] -= b0;
+    }
+    if (slot_ids) {
+        std::vector<float4> tmp(d.n);
+        CUDA_TRY(cudaMemcpy(tmp.data(), pos + d.p_off, sizeof(float4) * d.n, cudaMemcpyDeviceToHost));
+        for (uint32_t i = 0; i < d.n; ++i) std::memcpy(&slot_ids[i], &tmp[i].w, 4);
+    }
+    return SPH_OK;
+}
+
+sph_status StepState::read_sort(uint32_t* keys, uint32_t* counts, uint32_t* starts, uint32_t* order)
+{
+    if (scenes.empty()) return SPH_ERR_NOT_INITIALIZED;
+    const SceneDesc& d = scenes[0];
+    CUDA_TRY(cudaStreamSynchronize(stream_));
+    if (keys && d.n)   // keys are indexed by upload slot = input order
+        CUDA_TRY(cudaMemcpy(keys, key + d.p_off, sizeof(uint32_t) * d.n, cudaMemcpyDeviceToHost));
+    std::vector<uint32_t> table(d.buckets + 1ull);
+    CUDA_TRY(cudaMemcpy(table.data(), start + d.q_off, sizeof(uint32_t) * table.size(), cudaMemcpyDeviceToHost));
+    const uint32_t b0 = table[0];
+    for (auto& v : table) v -= b0;
+    if (starts) std::memcpy(starts, table.data(), sizeof(uint32_t) * table.size());
+    if (counts)
+        for (uint32_t b = 0; b < d.buckets; ++b) counts[b] = table[b + 1] - table[b];
+    if (order && d.n) {
+        std::vector<float4> tmp(d.n);
+        CUDA_TRY(cudaMemcpy(tmp.data(), pos + d.p_off, sizeof(float4) * d.n, cudaMemcpyDeviceToHost));
+        for (uint32_t i = 0; i < d.n; ++i) std::memcpy(&order[i], &tmp[i].w, 4);
+    }
+    return check_device_error();
+}
+
+}  // namespace sph

@@ -1,0 +1,232 @@
+"""Python face of the C ABI: the engine, the counting-sort stage and the batch.
+
+``SimulationEngineCUDA`` keeps the reference's engine vocabulary
+(SPHFluidSimulation/include/SPH/Core/SimulationEngine.h:35-76):
+``clear``, ``initialize``, ``update``, ``system_implementation_name``,
+``get_simulation_time``, plus readback of the dynamic and static particle
+buffers.  Every call goes through libsph_gb300.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import SphParams, check
+
+# the reference's 32-byte DynamicParticle (Particles.h:9-17)
+DYN_DTYPE = np.dtype([("pos", "<f4", 3), ("pressure", "<f4"), ("vel", "<f4", 3), ("hash", "<u4")])
+STATIC_DTYPE = np.dtype([("pos", "<f4", 3), ("pressure", "<f4")])
+
+
+def _fptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _uptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_uint32))
+
+
+def make_params(p) -> SphParams:
+    """From a ``scenes.Params`` (or anything with the same fields)."""
+    g = p.gravity
+    return SphParams(p.particle_mass, p.gas_constant, p.elasticity, p.viscosity, g[0], g[1], g[2],
+                     p.rest_density, p.h)
+
+
+def _f32(a, cols: int) -> Optional[np.ndarray]:
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, np.float32)
+    if a.size == 0:
+        return None
+    return a.reshape(-1, cols)
+
+
+class SimulationEngineCUDA:
+    """SPH step engine on one GPU (reference SimulationEngineCPU's interface)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _lib.load()
+        h = C.c_void_p()
+        check(self.lib.sph_engine_create(C.byref(h), int(device)), "sph_engine_create")
+        self.h = h
+        self.n = 0
+        self.s = 0
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.sph_engine_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- SimulationEngine ----------------------------------------------------
+    @staticmethod
+    def system_implementation_name() -> str:
+        return _lib.load().sph_engine_implementation_name().decode()
+
+    def clear(self) -> None:
+        check(self.lib.sph_engine_clear(self.h), "sph_engine_clear")
+        self.n = self.s = 0
+
+    def initialize(self, scene, vel: Optional[np.ndarray] = None) -> None:
+        """``scene`` is a ``scenes.Scene`` (positions, statics, params, triangles)."""
+        dyn = _f32(scene.dyn_pos, 3)
+        st = _f32(scene.static_pos, 3)
+        tri = _f32(scene.triangles, 9)
+        v = _f32(vel if vel is not None else scene.dyn_vel, 3)
+        p = make_params(scene.params)
+        n = 0 if dyn is None else dyn.shape[0]
+        s = 0 if st is None else st.shape[0]
+        t = 0 if tri is None else tri.shape[0]
+        check(self.lib.sph_engine_initialize(self.h, C.byref(p), _fptr(dyn), _fptr(v), n, _fptr(st), s,
+                                             _fptr(tri), t, float(scene.reorder_interval)),
+              "sph_engine_initialize")
+        self.n, self.s = n, s
+
+    def update(self, dt: float, steps: int) -> None:
+        check(self.lib.sph_engine_update(self.h, float(dt), int(steps)), "sph_engine_update")
+
+    def update_async(self, dt: float, steps: int) -> None:
+        check(self.lib.sph_engine_update_async(self.h, float(dt), int(steps)), "sph_engine_update_async")
+
+    def synchronize(self) -> None:
+        check(self.lib.sph_engine_synchronize(self.h), "sph_engine_synchronize")
+
+    def get_simulation_time(self) -> float:
+        t = C.c_double()
+        check(self.lib.sph_engine_simulation_time(self.h, C.byref(t)), "sph_engine_simulation_time")
+        return t.value
+
+    # -- buffers ---------------------------------------------------------------
+    def read_dynamic(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        if out is None:
+            out = np.zeros(self.n, DYN_DTYPE)
+        check(self.lib.sph_engine_read_dynamic(self.h, out.ctypes.data_as(C.c_void_p)), "sph_engine_read_dynamic")
+        return out
+
+    def write_dynamic(self, particles: np.ndarray) -> None:
+        p = np.ascontiguousarray(particles, DYN_DTYPE)
+        check(self.lib.sph_engine_write_dynamic(self.h, p.ctypes.data_as(C.c_void_p)), "sph_engine_write_dynamic")
+
+    def read_static(self):
+        out = np.zeros(self.s, STATIC_DTYPE)
+        starts = np.zeros(self.s + 1, np.uint32)
+        check(self.lib.sph_engine_read_static(self.h, out.ctypes.data_as(C.c_void_p), _uptr(starts)),
+              "sph_engine_read_static")
+        return out, starts
+
+    def read_buckets(self):
+        """(bucket_starts[2n+1], slot_ids[n]) in the reference's hashMap sense."""
+        starts = np.zeros(2 * self.n + 1, np.uint32)
+        ids = np.zeros(self.n, np.uint32)
+        check(self.lib.sph_engine_read_buckets(self.h, _uptr(starts), _uptr(ids)), "sph_engine_read_buckets")
+        return starts, ids
+
+    def record_acceleration(self, on: bool = True) -> None:
+        check(self.lib.sph_engine_record_acceleration(self.h, int(on)), "sph_engine_record_acceleration")
+
+    def read_acceleration(self) -> np.ndarray:
+        out = np.zeros((self.n, 3), np.float32)
+        check(self.lib.sph_engine_read_acceleration(self.h, _fptr(out)), "sph_engine_read_acceleration")
+        return out
+
+    def stream_handle(self) -> int:
+        """The engine's cudaStream_t as an integer."""
+        st = C.c_void_p()
+        check(self.lib.sph_engine_get_stream(self.h, C.byref(st)), "sph_engine_get_stream")
+        return st.value or 0
+
+    def set_timing(self, on: bool = True) -> None:
+        check(self.lib.sph_engine_set_timing(self.h, int(on)), "sph_engine_set_timing")
+
+    def kernel_times(self) -> np.ndarray:
+        ms = np.zeros(5, np.float32)
+        check(self.lib.sph_engine_kernel_times(self.h, _fptr(ms), 5), "sph_engine_kernel_times")
+        return ms
+
+
+def cell_sort(pos: np.ndarray, h: float, buckets: int, device: int = 0):
+    """The counting-sort stage alone: (keys, counts, starts, order)."""
+    lib = _lib.load()
+    p = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+    n = p.shape[0]
+    keys = np.zeros(n, np.uint32)
+    counts = np.zeros(buckets, np.uint32)
+    starts = np.zeros(buckets + 1, np.uint32)
+    order = np.zeros(n, np.uint32)
+    check(lib.sph_cell_sort(int(device), _fptr(p), n, float(h), int(buckets), _uptr(keys), _uptr(counts),
+                            _uptr(starts), _uptr(order)), "sph_cell_sort")
+    return keys, counts, starts, order
+
+
+class Batch:
+    """Many independent scenes advanced together (one persistent launch per step)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _lib.load()
+        h = C.c_void_p()
+        check(self.lib.sph_batch_create(C.byref(h), int(device)), "sph_batch_create")
+        self.h = h
+        self.sizes = []
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.sph_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_scene(self, scene, dt: Optional[float] = None) -> int:
+        dyn = _f32(scene.dyn_pos, 3)
+        st = _f32(scene.static_pos, 3)
+        tri = _f32(scene.triangles, 9)
+        v = _f32(scene.dyn_vel, 3)
+        p = make_params(scene.params)
+        sid = C.c_uint32()
+        check(self.lib.sph_batch_add_scene(self.h, C.byref(p), _fptr(dyn), _fptr(v), 0 if dyn is None else dyn.shape[0],
+                                           _fptr(st), 0 if st is None else st.shape[0], _fptr(tri),
+                                           0 if tri is None else tri.shape[0],
+                                           float(scene.dt if dt is None else dt), C.byref(sid)),
+              "sph_batch_add_scene")
+        self.sizes.append(0 if dyn is None else dyn.shape[0])
+        return sid.value
+
+    def finalize(self) -> None:
+        check(self.lib.sph_batch_finalize(self.h), "sph_batch_finalize")
+
+    def set_mode(self, mode: int) -> None:
+        check(self.lib.sph_batch_set_mode(self.h, int(mode)), "sph_batch_set_mode")
+
+    def step(self, steps: int = 1) -> None:
+        check(self.lib.sph_batch_step(self.h, int(steps)), "sph_batch_step")
+
+    def read_scene(self, scene_id: int) -> np.ndarray:
+        out = np.zeros(self.sizes[scene_id], DYN_DTYPE)
+        check(self.lib.sph_batch_read_scene(self.h, int(scene_id), out.ctypes.data_as(C.c_void_p)),
+              "sph_batch_read_scene")
+        return out
+
+    def info(self):
+        tot = C.c_uint64()
+        grid = C.c_uint32()
+        thr = C.c_uint32()
+        check(self.lib.sph_batch_info(self.h, C.byref(tot), C.byref(grid), C.byref(thr)), "sph_batch_info")
+        return tot.value, grid.value, thr.value

@@ -1,0 +1,254 @@
+"""ctypes access to the CPU oracle (test infrastructure).
+
+``Oracle`` wraps oracle/sph_oracle.c (float or double build); ``RefEngine``
+wraps oracle/_ref/libsph_ref.so, the reference's own SPHFunctions.cpp compiled
+from source, when that library exists (only where the reference tree is
+present).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from typing import Optional
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+_F32 = os.path.join(ORACLE_DIR, "_build", "libsph_oracle_f32.so")
+_F64 = os.path.join(ORACLE_DIR, "_build", "libsph_oracle_f64.so")
+REF_SO = os.path.join(ORACLE_DIR, "_ref", "libsph_ref.so")
+
+_fp = C.POINTER(C.c_float)
+_dp = C.POINTER(C.c_double)
+_up = C.POINTER(C.c_uint32)
+_vp = C.c_void_p
+
+# numpy dtype of the reference's 32-byte DynamicParticle (SF:12-16)
+DYN_DTYPE = np.dtype([("pos", "<f4", 3), ("pressure", "<f4"), ("vel", "<f4", 3), ("hash", "<u4")])
+
+
+def build_oracle() -> None:
+    subprocess.run(["make", "-s", "-C", ORACLE_DIR], check=True)
+
+
+def _ptr(a: Optional[np.ndarray], t):
+    if a is None:
+        return None
+    return a.ctypes.data_as(t)
+
+
+def _load(path: str):
+    if not os.path.exists(path):
+        build_oracle()
+    lib = C.CDLL(path)
+    lib.sph_oracle_create.restype = _vp
+    lib.sph_oracle_create.argtypes = [C.c_int]
+    lib.sph_oracle_destroy.argtypes = [_vp]
+    lib.sph_oracle_init.restype = C.c_int
+    lib.sph_oracle_init.argtypes = [_vp, _fp, _fp, _fp, C.c_uint32, _fp, C.c_uint32, _fp, C.c_uint32,
+                                    C.c_float, C.c_int]
+    lib.sph_oracle_update.restype = C.c_int
+    lib.sph_oracle_update.argtypes = [_vp, C.c_float, C.c_uint32]
+    lib.sph_oracle_record_accel.argtypes = [_vp, C.c_int]
+    lib.sph_oracle_count.restype = C.c_uint32
+    lib.sph_oracle_count.argtypes = [_vp, C.c_int]
+    lib.sph_oracle_sim_time.restype = C.c_double
+    lib.sph_oracle_sim_time.argtypes = [_vp]
+    lib.sph_oracle_read_dynamic.argtypes = [_vp, _dp]
+    lib.sph_oracle_read_raw.restype = C.c_int
+    lib.sph_oracle_read_raw.argtypes = [_vp, _vp]
+    lib.sph_oracle_read_maps.argtypes = [_vp, _up, _up, _up]
+    lib.sph_oracle_read_static.argtypes = [_vp, _dp, _up]
+    lib.sph_oracle_read_accel.argtypes = [_vp, _dp]
+    lib.sph_oracle_derived.argtypes = [_vp, _dp, _dp]
+    lib.sph_oracle_hash.argtypes = [_fp, C.c_uint32, C.c_float, C.c_uint32, _up]
+    lib.sph_oracle_counting_sort.argtypes = [_up, C.c_uint32, C.c_uint32, _up, _up, _up]
+    return lib
+
+
+_LIBS = {}
+
+
+def lib(double: bool = False):
+    key = "f64" if double else "f32"
+    if key not in _LIBS:
+        _LIBS[key] = _load(_F64 if double else _F32)
+    return _LIBS[key]
+
+
+class Oracle:
+    """The reference CPU engine restated: Initialize / Update / readback."""
+
+    def __init__(self, threads: int = 0, double: bool = False):
+        self.lib = lib(double)
+        self.double = double
+        self.h = self.lib.sph_oracle_create(int(threads))
+
+    def __del__(self):
+        try:
+            self.lib.sph_oracle_destroy(self.h)
+        except Exception:
+            pass
+
+    def init(self, scene, vel: Optional[np.ndarray] = None, parallel_partial_sum: bool = False) -> None:
+        p9 = scene.params.as9()
+        dyn = np.ascontiguousarray(scene.dyn_pos, np.float32)
+        st = np.ascontiguousarray(scene.static_pos, np.float32)
+        tri = np.ascontiguousarray(scene.triangles, np.float32)
+        v = None if vel is None else np.ascontiguousarray(vel, np.float32)
+        rc = self.lib.sph_oracle_init(self.h, _ptr(p9, _fp), _ptr(dyn, _fp), _ptr(v, _fp), dyn.shape[0],
+                                      _ptr(st, _fp), st.shape[0], _ptr(tri, _fp), tri.shape[0],
+                                      float(scene.reorder_interval), int(parallel_partial_sum))
+        assert rc == 0
+
+    def update(self, dt: float, steps: int) -> None:
+        assert self.lib.sph_oracle_update(self.h, float(dt), int(steps)) == 0
+
+    def record_accel(self, on: bool = True) -> None:
+        self.lib.sph_oracle_record_accel(self.h, int(on))
+
+    @property
+    def n(self) -> int:
+        return self.lib.sph_oracle_count(self.h, 0)
+
+    @property
+    def s(self) -> int:
+        return self.lib.sph_oracle_count(self.h, 1)
+
+    @property
+    def buckets(self) -> int:
+        return self.lib.sph_oracle_count(self.h, 2)
+
+    def sim_time(self) -> float:
+        return self.lib.sph_oracle_sim_time(self.h)
+
+    def read(self) -> np.ndarray:
+        """(N, 8) float64: px, py, pz, pressure, vx, vy, vz, hash (slot order)."""
+        out = np.zeros((self.n, 8), np.float64)
+        self.lib.sph_oracle_read_dynamic(self.h, _ptr(out, _dp))
+        return out
+
+    def read_raw(self) -> np.ndarray:
+        out = np.zeros(self.n, DYN_DTYPE)
+        assert self.lib.sph_oracle_read_raw(self.h, out.ctypes.data) == 0
+        return out
+
+    def maps(self):
+        """(hash_map[B+1], particle_map[N], init_order[N]) -- init_order[slot]
+        is the input index of the particle in that buffer slot."""
+        hm = np.zeros(self.buckets + 1, np.uint32)
+        pm = np.zeros(self.n, np.uint32)
+        io = np.zeros(self.n, np.uint32)
+        self.lib.sph_oracle_read_maps(self.h, _ptr(hm, _up), _ptr(pm, _up), _ptr(io, _up))
+        return hm, pm, io
+
+    def statics(self):
+        pos = np.zeros((self.s, 4), np.float64)
+        sm = np.zeros(self.s + 1, np.uint32)
+        self.lib.sph_oracle_read_static(self.h, _ptr(pos, _dp), _ptr(sm, _up))
+        return pos, sm
+
+    def accel(self) -> np.ndarray:
+        a = np.zeros((self.n, 3), np.float64)
+        self.lib.sph_oracle_read_accel(self.h, _ptr(a, _dp))
+        return a
+
+    def derived(self):
+        sd, kc = C.c_double(), C.c_double()
+        self.lib.sph_oracle_derived(self.h, C.byref(sd), C.byref(kc))
+        return sd.value, kc.value
+
+    def by_input_order(self) -> np.ndarray:
+        """Current particle state (N, 8) re-indexed by input particle."""
+        st = self.read()
+        _, _, io = self.maps()
+        out = np.empty_like(st)
+        out[io] = st
+        return out
+
+
+def oracle_hash(pos: np.ndarray, h: float, buckets: int) -> np.ndarray:
+    p = np.ascontiguousarray(pos, np.float32)
+    keys = np.zeros(p.shape[0], np.uint32)
+    lib().sph_oracle_hash(_ptr(p, _fp), p.shape[0], float(h), int(buckets), _ptr(keys, _up))
+    return keys
+
+
+def oracle_counting_sort(keys: np.ndarray, buckets: int):
+    k = np.ascontiguousarray(keys, np.uint32)
+    counts = np.zeros(buckets, np.uint32)
+    starts = np.zeros(buckets + 1, np.uint32)
+    pm = np.zeros(k.shape[0], np.uint32)
+    lib().sph_oracle_counting_sort(_ptr(k, _up), k.shape[0], int(buckets), _ptr(counts, _up),
+                                   _ptr(starts, _up), _ptr(pm, _up))
+    return counts, starts, pm
+
+
+class RefEngine:
+    """The reference's own SPHFunctions.cpp, compiled from source (only where
+    the reference tree is present)."""
+
+    def __init__(self):
+        if not os.path.exists(REF_SO):
+            raise FileNotFoundError(REF_SO)
+        L = C.CDLL(REF_SO)
+        L.sph_ref_create.restype = _vp
+        L.sph_ref_destroy.argtypes = [_vp]
+        L.sph_ref_init.restype = C.c_int
+        L.sph_ref_init.argtypes = [_vp, _fp, _fp, _fp, C.c_uint32, _fp, C.c_uint32, _fp, C.c_uint32, C.c_float]
+        L.sph_ref_update.restype = C.c_int
+        L.sph_ref_update.argtypes = [_vp, C.c_float, C.c_uint32]
+        L.sph_ref_read_raw.argtypes = [_vp, _vp]
+        L.sph_ref_read_maps.argtypes = [_vp, _up, _up, _up]
+        L.sph_ref_read_static.argtypes = [_vp, _fp, _up]
+        L.sph_ref_hash.argtypes = [_fp, C.c_uint32, C.c_float, C.c_uint32, _up]
+        self.L = L
+        self.h = L.sph_ref_create()
+        self.n = 0
+        self.s = 0
+
+    def __del__(self):
+        try:
+            self.L.sph_ref_destroy(self.h)
+        except Exception:
+            pass
+
+    def init(self, scene, vel: Optional[np.ndarray] = None) -> None:
+        p9 = scene.params.as9()
+        dyn = np.ascontiguousarray(scene.dyn_pos, np.float32)
+        st = np.ascontiguousarray(scene.static_pos, np.float32)
+        tri = np.ascontiguousarray(scene.triangles, np.float32)
+        v = None if vel is None else np.ascontiguousarray(vel, np.float32)
+        assert self.L.sph_ref_init(self.h, _ptr(p9, _fp), _ptr(dyn, _fp), _ptr(v, _fp), dyn.shape[0],
+                                   _ptr(st, _fp), st.shape[0], _ptr(tri, _fp), tri.shape[0],
+                                   float(scene.reorder_interval)) == 0
+        self.n, self.s = dyn.shape[0], st.shape[0]
+
+    def update(self, dt: float, steps: int) -> None:
+        assert self.L.sph_ref_update(self.h, float(dt), int(steps)) == 0
+
+    def read_raw(self) -> np.ndarray:
+        out = np.zeros(self.n, DYN_DTYPE)
+        self.L.sph_ref_read_raw(self.h, out.ctypes.data)
+        return out
+
+    def maps(self):
+        hm = np.zeros(2 * self.n + 1, np.uint32)
+        pm = np.zeros(self.n, np.uint32)
+        io = np.zeros(self.n, np.uint32)
+        self.L.sph_ref_read_maps(self.h, _ptr(hm, _up), _ptr(pm, _up), _ptr(io, _up))
+        return hm, pm, io
+
+    def statics(self):
+        pos = np.zeros((self.s, 4), np.float32)
+        sm = np.zeros(self.s + 1, np.uint32)
+        self.L.sph_ref_read_static(self.h, _ptr(pos, _fp), _ptr(sm, _up))
+        return pos, sm
+
+    def hash(self, pos: np.ndarray, h: float, mod: int) -> np.ndarray:
+        p = np.ascontiguousarray(pos, np.float32)
+        keys = np.zeros(p.shape[0], np.uint32)
+        self.L.sph_ref_hash(_ptr(p, _fp), p.shape[0], float(h), int(mod), _ptr(keys, _up))
+        return keys

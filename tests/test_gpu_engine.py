@@ -1,0 +1,275 @@
+"""GPU engine parity against the oracle (the reference CPU step restated and
+pinned bit-exact to the reference's own code) and its FP64 rerun.
+
+Tolerances (stated by the spec for FP32 parity):
+  density   |rho_gpu - rho_ref| / rho_ref <= 1e-5 per particle, one step
+  force     |a_gpu - a_ref| <= 1e-4 * max_i |a_ref|, one step
+  position  RMS over particles of |x_gpu - x_ref| <= 1e-3 * h after 50 steps
+Each is also reported against the FP64 rerun of the reference step.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from oracle_lib import Oracle, oracle_hash
+from sphfluidsimulation_gb300 import scenes
+from sphfluidsimulation_gb300._lib import SphError
+from sphfluidsimulation_gb300.engine import SimulationEngineCUDA
+
+pytestmark = pytest.mark.gpu
+
+RHO_TOL = 1e-5
+ACC_TOL = 1e-4
+POS_TOL = 1e-3
+
+
+def density(p, gas, rho0):
+    """The reference keeps pressure only; density = p / k + rho0 (SF:544)."""
+    return p / gas + rho0
+
+
+def gpu_state(eng):
+    d = eng.read_dynamic()
+    return d
+
+
+def small_scene():
+    return scenes.dam_break((20, 12, 20), 0.02, 0.04, (0.6, 0.4, 0.6), 0, mass=0.008, name="dam_4800")
+
+
+def run_pair(sc, steps, vel=None, record=False):
+    o = Oracle(0)
+    o.init(sc, vel)
+    d = Oracle(0, double=True)
+    d.init(sc, vel)
+    e = SimulationEngineCUDA()
+    e.initialize(sc, vel)
+    if record:
+        o.record_accel(True)
+        d.record_accel(True)
+        e.record_acceleration(True)
+    o.update(sc.dt, steps)
+    d.update(sc.dt, steps)
+    e.update(sc.dt, steps)
+    return o, d, e
+
+
+def by_input(o):
+    st = o.read()
+    _, _, io = o.maps()
+    out = np.empty_like(st)
+    out[io] = st
+    return out, io
+
+
+def test_one_step_density_pressure_and_force():
+    sc = small_scene()
+    o, d, e = run_pair(sc, 1, record=True)
+    ref, io = by_input(o)
+    ref64, io64 = by_input(d)
+    g = gpu_state(e)
+    gas, rho0 = sc.params.gas_constant, sc.params.rest_density
+    rho_ref = density(ref[:, 3], gas, rho0)
+    rho_64 = density(ref64[:, 3], gas, rho0)
+    rho_gpu = density(g["pressure"].astype(np.float64), gas, rho0)
+    err = np.abs(rho_gpu - rho_ref) / rho_ref
+    err64 = np.abs(rho_gpu - rho_64) / rho_64
+    ref_err64 = np.abs(rho_ref - rho_64) / rho_64
+    print(f"density rel err: vs fp32 {err.max():.3e}, vs fp64 {err64.max():.3e}, fp32 ref vs fp64 {ref_err64.max():.3e}")
+    assert err.max() <= RHO_TOL
+    # acceleration F/rho + g (slot order -> input order)
+    a_ref = np.empty((sc.n, 3))
+    a_ref[io] = o.accel()
+    a64 = np.empty((sc.n, 3))
+    a64[io64] = d.accel()
+    a_gpu = e.read_acceleration().astype(np.float64)
+    scale = np.abs(a_ref).max()
+    ferr = np.abs(a_gpu - a_ref).max() / scale
+    ferr64 = np.abs(a_gpu - a64).max() / np.abs(a64).max()
+    print(f"force err / max|a|: vs fp32 {ferr:.3e}, vs fp64 {ferr64:.3e}")
+    assert ferr <= ACC_TOL
+    # hashes stored with the particles are the keys of their positions
+    keys = oracle_hash(np.stack(list(g["pos"].T), 1), sc.params.h, 2 * sc.n)
+    assert np.array_equal(keys, g["hash"])
+
+
+def test_stagewise_one_step_from_oracle_state():
+    """Feed the oracle's state after k steps to a fresh GPU engine and
+    compare one step (the error of one step, not accumulated)."""
+    sc = small_scene()
+    o = Oracle(0)
+    o.init(sc)
+    o.update(sc.dt, 30)
+    st, _ = by_input(o)
+    pos = st[:, :3].astype(np.float32)
+    vel = st[:, 4:7].astype(np.float32)
+    sc2 = scenes.Scene(name="k30", dyn_pos=pos, static_pos=sc.static_pos, params=sc.params, dt=sc.dt, steps=1)
+    o2, d2, e2 = run_pair(sc2, 1, vel=vel, record=True)
+    ref, io = by_input(o2)
+    g = gpu_state(e2)
+    gas, rho0 = sc.params.gas_constant, sc.params.rest_density
+    err = np.abs(density(g["pressure"].astype(np.float64), gas, rho0) - density(ref[:, 3], gas, rho0)) / density(ref[:, 3], gas, rho0)
+    assert err.max() <= RHO_TOL
+    a_ref = np.empty((sc.n, 3))
+    a_ref[io] = o2.accel()
+    assert np.abs(e2.read_acceleration() - a_ref).max() <= ACC_TOL * np.abs(a_ref).max()
+    dx = np.asarray(g["pos"], np.float64) - ref[:, :3]
+    assert np.sqrt((dx ** 2).sum(1).mean()) <= 1e-6 * sc.params.h * 1000
+
+
+def test_fifty_step_trajectory_rms():
+    sc = small_scene()
+    o, d, e = run_pair(sc, 50)
+    ref, _ = by_input(o)
+    ref64, _ = by_input(d)
+    g = gpu_state(e)
+    x = np.asarray(g["pos"], np.float64)
+    rms = np.sqrt(((x - ref[:, :3]) ** 2).sum(1).mean())
+    rms64 = np.sqrt(((x - ref64[:, :3]) ** 2).sum(1).mean())
+    ref_rms64 = np.sqrt(((ref[:, :3] - ref64[:, :3]) ** 2).sum(1).mean())
+    h = sc.params.h
+    print(f"50-step RMS / h: vs fp32 {rms / h:.3e}, vs fp64 {rms64 / h:.3e}, fp32 ref vs fp64 {ref_rms64 / h:.3e}")
+    assert rms <= POS_TOL * h
+
+
+def test_bucket_table_invariants_after_steps():
+    """The reference's DebugHashAndParticleMap checks on the GPU state."""
+    sc = small_scene()
+    e = SimulationEngineCUDA()
+    e.initialize(sc)
+    for _ in range(3):
+        e.update(sc.dt, 7)
+        starts, ids = e.read_buckets()
+        n, B = sc.n, 2 * sc.n
+        assert starts[0] == 0 and starts[B] == n
+        assert (np.diff(starts.astype(np.int64)) >= 0).all()
+        assert np.array_equal(np.sort(ids), np.arange(n, dtype=np.uint32))
+        g = gpu_state(e)
+        keys = g["hash"][ids]
+        b_of_slot = np.repeat(np.arange(B), np.diff(starts.astype(np.int64)))
+        assert np.array_equal(keys, b_of_slot)
+
+
+def test_static_particles_sorted_like_reference():
+    sc = small_scene()
+    o = Oracle(0)
+    o.init(sc)
+    e = SimulationEngineCUDA()
+    e.initialize(sc)
+    sp, table = e.read_static()
+    rsp, rtable = o.statics()
+    assert np.array_equal(table, rtable)
+    for b in np.nonzero(np.diff(rtable.astype(np.int64)))[0][:200]:
+        a = {tuple(v) for v in sp["pos"][table[b]:table[b + 1]]}
+        r = {tuple(v) for v in rsp[rtable[b]:rtable[b + 1], :3].astype(np.float32)}
+        assert a == r
+
+
+@pytest.mark.parametrize("name", ["debug_smallest", "small_dam", "negative_cells", "triangles"])
+def test_reference_golden_fixtures(name):
+    """The reference's own outputs (tests/golden) at each checkpoint."""
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", f"{name}.npz"))
+    p = z["params9"]
+    params = scenes.Params(*[float(v) for v in p[:4]], (float(p[4]), float(p[5]), float(p[6])), float(p[7]), float(p[8]))
+    sc = scenes.Scene(name=name, dyn_pos=z["dyn_pos"], static_pos=z["static_pos"], params=params,
+                      dt=float(z["dt"]), steps=0, triangles=z["triangles"])
+    e = SimulationEngineCUDA()
+    e.initialize(sc)
+    io = z["init_order"]
+    done = 0
+    h = params.h
+    for k, c in enumerate(z["checkpoints"]):
+        e.update(sc.dt, int(c) - done)
+        done = int(c)
+        raw = z[f"particles_{k}"].view(np.float32).reshape(-1, 8)
+        ref = np.empty_like(raw)
+        ref[io] = raw
+        g = gpu_state(e)
+        rho_ref = density(ref[:, 3].astype(np.float64), params.gas_constant, params.rest_density)
+        rho_gpu = density(g["pressure"].astype(np.float64), params.gas_constant, params.rest_density)
+        rms = np.sqrt(((np.asarray(g["pos"], np.float64) - ref[:, :3]) ** 2).sum(1).mean())
+        assert rms <= POS_TOL * h, (c, rms / h)
+        if int(c) == 1:
+            assert (np.abs(rho_gpu - rho_ref) / np.abs(rho_ref)).max() <= RHO_TOL
+
+
+def test_empty_and_static_only_scenes():
+    e = SimulationEngineCUDA()
+    sc = small_scene()
+    empty = scenes.Scene(name="empty", dyn_pos=np.zeros((0, 3), np.float32), static_pos=sc.static_pos,
+                         params=sc.params, dt=sc.dt, steps=1)
+    e.initialize(empty)
+    e.update(sc.dt, 3)
+    assert e.read_dynamic().shape == (0,)
+    sp, table = e.read_static()
+    assert sp.shape[0] == sc.s and table[-1] == sc.s
+    none = scenes.Scene(name="none", dyn_pos=np.zeros((0, 3), np.float32), static_pos=np.zeros((0, 3), np.float32),
+                        params=sc.params, dt=sc.dt, steps=1)
+    e.initialize(none)
+    e.update(sc.dt, 1)
+
+
+def test_update_before_initialize_is_an_error():
+    e = SimulationEngineCUDA()
+    with pytest.raises(SphError) as ei:
+        e.update(1e-4, 1)
+    assert ei.value.status == 2
+
+
+def test_invalid_arguments_rejected():
+    e = SimulationEngineCUDA()
+    sc = small_scene()
+    sc.params.h = 0.0
+    with pytest.raises(SphError) as ei:
+        e.initialize(sc)
+    assert ei.value.status == 1
+
+
+def test_simulation_time_and_name():
+    e = SimulationEngineCUDA()
+    sc = small_scene()
+    e.initialize(sc)
+    e.update(1e-4, 10)
+    e.update(2e-4, 5)
+    assert abs(e.get_simulation_time() - 2e-3) < 1e-12
+    assert SimulationEngineCUDA.system_implementation_name() == "CUDA-sm_103a"
+
+
+def test_write_dynamic_round_trip_and_restart():
+    sc = small_scene()
+    a = SimulationEngineCUDA()
+    a.initialize(sc)
+    a.update(sc.dt, 5)
+    state = a.read_dynamic()
+    b = SimulationEngineCUDA()
+    b.initialize(sc)
+    b.write_dynamic(state)
+    assert np.array_equal(b.read_dynamic()[["pos", "vel"]], state[["pos", "vel"]])
+    a.update(sc.dt, 3)
+    b.update(sc.dt, 3)
+    x = np.asarray(a.read_dynamic()["pos"], np.float64)
+    y = np.asarray(b.read_dynamic()["pos"], np.float64)
+    assert np.sqrt(((x - y) ** 2).sum(1).mean()) <= 1e-5 * sc.params.h
+
+
+def test_deterministic_repeat():
+    sc = small_scene()
+    out = []
+    for _ in range(2):
+        e = SimulationEngineCUDA()
+        e.initialize(sc)
+        e.update(sc.dt, 20)
+        out.append(e.read_dynamic().tobytes())
+    assert out[0] == out[1]
+
+
+def test_kernel_timing_reported():
+    sc = small_scene()
+    e = SimulationEngineCUDA()
+    e.initialize(sc)
+    e.set_timing(True)
+    e.update(sc.dt, 3)
+    t = e.kernel_times()
+    assert (t > 0).all()

@@ -1,0 +1,92 @@
+"""GPU counting sort (hash + count + scan + stable scatter) against the oracle:
+keys, per-bucket counts and bucket starts bit-exact, per-bucket membership
+equal, and the within-bucket order stable (ascending input index)."""
+import numpy as np
+import pytest
+
+from oracle_lib import Oracle, oracle_counting_sort, oracle_hash
+from sphfluidsimulation_gb300 import scenes
+from sphfluidsimulation_gb300.engine import cell_sort
+
+pytestmark = pytest.mark.gpu
+
+
+def check_sort(pos, h, buckets):
+    pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+    keys, counts, starts, order = cell_sort(pos, h, buckets)
+    ref_keys = oracle_hash(pos, h, buckets)
+    assert np.array_equal(keys, ref_keys), "keys"
+    ref_counts, ref_starts, ref_pm = oracle_counting_sort(ref_keys, buckets)
+    assert np.array_equal(counts, ref_counts), "counts"
+    assert np.array_equal(starts, ref_starts), "bucket starts"
+    # same members per bucket as the reference's particleMap; ascending order
+    expect = np.argsort(ref_keys, kind="stable").astype(np.uint32)
+    assert np.array_equal(order, expect), "membership / stability"
+    for b in np.nonzero(ref_counts)[0][:50]:
+        assert set(order[starts[b]:starts[b + 1]]) == set(ref_pm[ref_starts[b]:ref_starts[b + 1]])
+    return keys, counts, starts, order
+
+
+def test_sort_config0_initial():
+    sc = scenes.config0(steps=1)
+    check_sort(sc.dyn_pos, sc.params.h, 2 * sc.n)
+
+
+def test_sort_oracle_positions_after_steps():
+    """Stage-wise: the oracle's own positions after 40 steps (some particles
+    have left the box, negative cells included)."""
+    sc = scenes.dam_break((16, 12, 16), 0.02, 0.04, (0.5, 0.4, 0.5), 0, mass=0.008)
+    o = Oracle(0)
+    o.init(sc)
+    o.update(sc.dt, 40)
+    st = o.read()
+    check_sort(st[:, :3].astype(np.float32), sc.params.h, 2 * sc.n)
+
+
+@pytest.mark.parametrize("buckets", [1, 7, 4096, 12345, 1 << 20, 2_000_003])
+def test_sort_random_positions_any_bucket_count(buckets):
+    rng = np.random.default_rng(buckets)
+    pos = rng.uniform(-3, 3, size=(5000, 3)).astype(np.float32)
+    check_sort(pos, 0.1, buckets)
+
+
+def test_sort_cell_boundaries_and_coincident():
+    h = np.float32(0.04)
+    k = np.arange(-20, 20, dtype=np.float32)
+    on = k * h
+    below = np.nextafter(on, np.float32(-np.inf))
+    above = np.nextafter(on, np.float32(np.inf))
+    xs = np.concatenate([on, below, above])
+    pos = np.stack(np.meshgrid(xs, xs[::7], xs[::11], indexing="ij"), -1).reshape(-1, 3)
+    pos = np.concatenate([pos, np.repeat(pos[:5], 50, axis=0)])   # coincident clusters
+    check_sort(pos, float(h), 2 * pos.shape[0])
+
+
+def test_sort_single_and_tiny():
+    check_sort(np.array([[0.5, 0.5, 0.5]], np.float32), 1.0, 2)
+    check_sort(np.array([[0.5, 0.5, 0.5], [0.5, 0.5, 0.5]], np.float32), 1.0, 4)
+
+
+def test_sort_ragged_tail_sizes():
+    rng = np.random.default_rng(1)
+    for n in (127, 128, 129, 255, 2049, 4097):
+        pos = rng.uniform(0, 1, size=(n, 3)).astype(np.float32)
+        check_sort(pos, 0.05, 2 * n)
+
+
+def test_sort_one_million_properties():
+    """Config-1 size: keys against the oracle, counts = bincount, starts
+    monotone with starts[B] = N, order a permutation sorted by key."""
+    sc = scenes.config1(steps=1)
+    pos = sc.dyn_pos
+    B = 2 * sc.n
+    keys, counts, starts, order = cell_sort(pos, sc.params.h, B)
+    assert np.array_equal(keys, oracle_hash(pos, sc.params.h, B))
+    assert np.array_equal(counts, np.bincount(keys, minlength=B))
+    assert starts[0] == 0 and starts[B] == sc.n
+    assert np.array_equal(np.sort(order), np.arange(sc.n, dtype=np.uint32))
+    k_sorted = keys[order]
+    assert (np.diff(k_sorted.astype(np.int64)) >= 0).all()
+    # stability: inside each bucket the input indices ascend
+    same = np.diff(k_sorted.astype(np.int64)) == 0
+    assert (np.diff(order.astype(np.int64))[same] > 0).all()

@@ -1,0 +1,163 @@
+"""CPU oracle checks: the C restatement (oracle/sph_oracle.c) against the
+golden fixtures produced by the reference itself, the reference's own debug
+validators as invariants, threading and FP64 behaviour."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from oracle_lib import REF_SO, Oracle, RefEngine, oracle_counting_sort, oracle_hash
+from sphfluidsimulation_gb300 import scenes
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+
+
+class _FixtureScene:
+    def __init__(self, z):
+        p = z["params9"]
+        self.dyn_pos = z["dyn_pos"]
+        self.static_pos = z["static_pos"]
+        self.triangles = z["triangles"]
+        self.params = scenes.Params(float(p[0]), float(p[1]), float(p[2]), float(p[3]),
+                                    (float(p[4]), float(p[5]), float(p[6])), float(p[7]), float(p[8]))
+        self.dt = float(z["dt"])
+        self.reorder_interval = float(z["reorder_interval"])
+        self.dyn_vel = None
+
+
+def test_golden_fixtures_present():
+    names = {os.path.basename(p) for p in GOLDEN}
+    assert {"debug_smallest.npz", "small_dam.npz", "small_dam_reorder.npz", "negative_cells.npz",
+            "triangles.npz"} <= names
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
+def test_oracle_bit_exact_against_reference_fixtures(path):
+    """Every checkpoint: raw particle buffer, hashMap, particleMap, init
+    permutation and sorted statics equal the reference's, bit for bit."""
+    z = np.load(path)
+    sc = _FixtureScene(z)
+    o = Oracle(0)
+    o.init(sc)
+    hm, pm, io = o.maps()
+    assert np.array_equal(io, z["init_order"])
+    if sc.static_pos.shape[0]:
+        sp, sm = o.statics()
+        assert np.array_equal(sp.astype(np.float32), z["static_sorted"])
+        assert np.array_equal(sm, z["static_map"])
+    done = 0
+    for k, c in enumerate(z["checkpoints"]):
+        o.update(sc.dt, int(c) - done)
+        done = int(c)
+        raw = o.read_raw().view(np.uint32).reshape(-1, 8)
+        assert np.array_equal(raw, z[f"particles_{k}"]), f"checkpoint {c}"
+        hm, pm, _ = o.maps()
+        assert np.array_equal(hm, z[f"hash_map_{k}"])
+        assert np.array_equal(pm, z[f"particle_map_{k}"])
+
+
+def _validate(o: Oracle):
+    """SimulationEngine.h validators: DebugParticles (hash of position, finite
+    values, :115-177), DebugPrePrefixSumHashes (:178-190) and
+    DebugHashAndParticleMap (:229-282)."""
+    st = o.read()
+    hm, pm, _ = o.maps()
+    n, B = o.n, o.buckets
+    assert np.isfinite(st[:, :7]).all()
+    keys = oracle_hash(st[:, :3].astype(np.float32), o.h_param, B)
+    assert np.array_equal(keys, st[:, 7].astype(np.uint32))
+    assert hm[0] == 0 and hm[B] == n
+    assert (np.diff(hm.astype(np.int64)) >= 0).all()
+    counts = np.bincount(keys, minlength=B)
+    assert np.array_equal(np.diff(hm.astype(np.int64)), counts)
+    b_of_slot = np.repeat(np.arange(B), counts)
+    assert np.array_equal(keys[pm], b_of_slot)
+
+
+def test_oracle_validators_hold_over_steps():
+    sc = scenes.dam_break((12, 10, 12), 0.02, 0.04, (0.5, 0.4, 0.5), 0, mass=0.008)
+    o = Oracle(0)
+    o.init(sc)
+    o.h_param = sc.params.h
+    for _ in range(5):
+        o.update(sc.dt, 4)
+        _validate(o)
+
+
+def test_threaded_oracle_matches_serial():
+    """T>0 threads: same counts and tables, particle state equal within FP32
+    summation-order noise (the bucket order is non-deterministic, as in the
+    reference)."""
+    sc = scenes.dam_break((12, 10, 12), 0.02, 0.04, (0.5, 0.4, 0.5), 0, mass=0.008)
+    a, b = Oracle(0), Oracle(4)
+    a.init(sc)
+    b.init(sc)
+    for steps in (1, 3):
+        a.update(sc.dt, steps)
+        b.update(sc.dt, steps)
+    sa, sb = a.by_input_order(), b.by_input_order()
+    assert np.abs(sa[:, :3] - sb[:, :3]).max() < 1e-6
+    assert np.abs(sa[:, 3] - sb[:, 3]).max() <= 1e-5 * 200 * 1000
+    ha, _, _ = a.maps()
+    hb, _, _ = b.maps()
+    assert np.array_equal(ha, hb)
+
+
+def test_parallel_partial_sum_matches():
+    sc = scenes.dam_break((12, 10, 12), 0.02, 0.04, (0.5, 0.4, 0.5), 0, mass=0.008)
+    a, b = Oracle(0), Oracle(3)
+    a.init(sc)
+    b.init(sc, parallel_partial_sum=True)
+    a.update(sc.dt, 2)
+    b.update(sc.dt, 2)
+    assert np.array_equal(a.maps()[0], b.maps()[0])
+
+
+def test_fp64_rerun_close_to_fp32():
+    sc = scenes.dam_break((12, 10, 12), 0.02, 0.04, (0.5, 0.4, 0.5), 0, mass=0.008)
+    a, b = Oracle(0), Oracle(0, double=True)
+    a.init(sc)
+    b.init(sc)
+    a.update(sc.dt, 1)
+    b.update(sc.dt, 1)
+    sa, sb = a.by_input_order(), b.by_input_order()
+    rho_a = sa[:, 3] / 200.0 + 1000.0
+    rho_b = sb[:, 3] / 200.0 + 1000.0
+    assert np.max(np.abs(rho_a - rho_b) / rho_b) < 1e-5
+
+
+def test_counting_sort_semantics():
+    rng = np.random.default_rng(3)
+    keys = rng.integers(0, 50, size=400).astype(np.uint32)
+    counts, starts, pm = oracle_counting_sort(keys, 50)
+    assert np.array_equal(counts, np.bincount(keys, minlength=50))
+    assert starts[0] == 0 and starts[50] == 400
+    for b in range(50):
+        members = pm[starts[b]:starts[b + 1]]
+        assert (keys[members] == b).all()
+        # the decrementing fill lists a bucket's members in descending order
+        assert (np.diff(members.astype(np.int64)) < 0).all()
+
+
+def test_hash_negative_cells_wrap():
+    pos = np.array([[-0.01, 0.0, 0.0], [0.0, -0.01, 0.0], [0.0, 0.0, -0.01]], np.float32)
+    keys = oracle_hash(pos, 1.0, 1 << 30)
+    ex = lambda v: int(''.join('00' + b for b in format(v & 1023, '010b')), 2)  # noqa: E731
+    assert keys[0] == ex(1023)
+    assert keys[1] == 2 * ex(1023)
+    assert keys[2] == 4 * ex(1023)
+
+
+@pytest.mark.skipif(not os.path.exists(REF_SO), reason="reference not compiled here (no reference tree)")
+def test_oracle_matches_reference_random_scene():
+    sc = scenes.dam_break((11, 9, 13), 0.02, 0.04, (0.5, 0.4, 0.5), 0, mass=0.008)
+    sc.dyn_pos = (sc.dyn_pos - np.float32(0.05)).astype(np.float32)
+    o, r = Oracle(0), RefEngine()
+    o.init(sc)
+    r.init(sc)
+    for steps in (1, 7):
+        o.update(sc.dt, steps)
+        r.update(sc.dt, steps)
+        assert o.read_raw().tobytes() == r.read_raw().tobytes()
+        assert all(np.array_equal(x, y) for x, y in zip(o.maps(), r.maps()))
