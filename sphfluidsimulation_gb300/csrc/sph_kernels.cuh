@@ -359,7 +359,7 @@ __device__ __forceinline__ void scatter_tile(const Tile& tile, const SceneDesc* 
 // a smaller source slot), so each bucket keeps the previous slot order: a
 // deterministic, stable counting sort.  Buckets hold a handful of particles,
 // so the rank loop reads a few words from L1.
-constexpr uint32_t kStableRankLimit = 4096;   // larger buckets keep arrival order
+constexpr uint32_t kStableRankLimit = 8192;   // larger buckets keep arrival order
 
 __device__ __forceinline__ void gather_tile(const Tile& tile, const SceneDesc* scenes, const uint32_t* key,
                                             const uint32_t* arrival, const uint32_t* perm, const uint32_t* start,

@@ -1,0 +1,390 @@
+// sph_server.cu -- continuous batching of simulation jobs on one GPU.
+//
+// The reference has no serving layer (it advances one scene per engine,
+// SimulationEngineCPU.cpp:420-459); this is the served form of the same step.
+// Jobs wait in a FIFO queue.  A job is admitted when its resident bytes fit
+// the HBM budget and a slot is free (queued jobs behind a job that does not
+// fit may pass it).  An admitted job is uploaded into its own ranges of one
+// device arena and sorted alone, so admissions and retirements never move
+// another job's state.  Every poll advances all admitted jobs together with
+// persistent step launches (one per step) over the current scene table, by
+// the smallest number of steps any of them still needs (at most chunk_steps),
+// so each job stops exactly at its horizon; finished jobs are read back and
+// their ranges freed.
+#include <algorithm>
+#include <chrono>
+#include <deque>
+#include <map>
+#include <memory>
+#include <new>
+#include <unordered_map>
+
+#include "sph_state.h"
+
+using sph::SceneDesc;
+using sph::SceneInput;
+using sph::StepState;
+
+namespace {
+
+constexpr uint64_t kAlign = 32;   // range starts: 128-byte aligned bucket tables
+
+// First-fit allocator over an index space [0, cap).
+class RangeAlloc {
+public:
+    void reset(uint64_t cap)
+    {
+        free_.clear();
+        cap_ = cap;
+        if (cap) free_[0] = cap;
+    }
+    uint64_t cap() const { return cap_; }
+    // Extends the space to new_cap (the tail becomes free).
+    void grow(uint64_t new_cap)
+    {
+        if (new_cap <= cap_) return;
+        uint64_t start = cap_, len = new_cap - cap_;
+        auto it = free_.lower_bound(start);
+        if (it != free_.begin()) {
+            auto prev = std::prev(it);
+            if (prev->first + prev->second == start) {
+                start = prev->first;
+                len += prev->second;
+                free_.erase(prev);
+            }
+        }
+        free_[start] = len;
+        cap_ = new_cap;
+    }
+    bool alloc(uint64_t len, uint64_t* off)
+    {
+        len = round(len);
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= len) {
+                *off = it->first;
+                const uint64_t rest = it->second - len;
+                const uint64_t at = it->first + len;
+                free_.erase(it);
+                if (rest) free_[at] = rest;
+                return true;
+            }
+        }
+        return false;
+    }
+    void release(uint64_t off, uint64_t len)
+    {
+        len = round(len);
+        auto it = free_.emplace(off, len).first;
+        auto next = std::next(it);
+        if (next != free_.end() && it->first + it->second == next->first) {
+            it->second += next->second;
+            free_.erase(next);
+        }
+        if (it != free_.begin()) {
+            auto prev = std::prev(it);
+            if (prev->first + prev->second == it->first) {
+                prev->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+    // Smallest capacity that would fit `len` more at the tail.
+    uint64_t needed_for(uint64_t len) const
+    {
+        len = round(len);
+        uint64_t tail_free = 0;
+        if (!free_.empty()) {
+            auto last = std::prev(free_.end());
+            if (last->first + last->second == cap_) tail_free = last->second;
+        }
+        return cap_ + (len > tail_free ? len - tail_free : 0);
+    }
+    static uint64_t round(uint64_t len) { return (std::max<uint64_t>(len, 1) + kAlign - 1) / kAlign * kAlign; }
+
+private:
+    std::map<uint64_t, uint64_t> free_;
+    uint64_t cap_ = 0;
+};
+
+enum class JobState { Queued, Active, Finished };
+
+struct Job {
+    uint64_t id = 0;
+    SceneInput in;
+    std::vector<float> pos, spos;
+    uint32_t steps = 0, done = 0;
+    JobState state = JobState::Queued;
+    uint64_t p_off = 0, q_off = 0, s_off = 0, sq_off = 0;
+    uint64_t bytes = 0;
+    std::vector<sph_dynamic_particle> result;
+    float gas = 1.f, rho0 = 0.f;
+};
+
+double now_s()
+{
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+uint64_t job_bytes(uint32_t n, uint32_t s)
+{
+    // per dynamic particle: sorted pos/vel 32, unsorted pos/vel 32, staging 32,
+    // key/arrival/perm 12, two buckets x (count + start) 16;
+    // per static particle: sorted 16, staging 32, bucket count + start 8
+    return 124ull * n + 56ull * s + 4096ull;
+}
+
+struct sph_server {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint64_t budget = 0;
+    uint32_t max_slots = 0;
+    StepState arena;
+    bool arena_ready = false;
+    RangeAlloc pa, qa, sa, sqa;
+    uint64_t used_bytes = 0;
+    uint64_t next_id = 1;
+    std::unordered_map<uint64_t, std::unique_ptr<Job>> jobs;
+    std::deque<uint64_t> queue;
+    std::vector<uint64_t> active;
+    bool dirty = false;
+};
+
+#define SRV_CUDA_TRY(expr)                                                                     \
+    do {                                                                                       \
+        cudaError_t e_ = (expr);                                                               \
+        if (e_ != cudaSuccess) {                                                               \
+            sph::set_last_error(std::string(#expr) + ": " + cudaGetErrorString(e_));           \
+            return e_ == cudaErrorMemoryAllocation ? SPH_ERR_OUT_OF_MEMORY : SPH_ERR_CUDA;     \
+        }                                                                                      \
+    } while (0)
+
+#define SRV_TRY(expr)                 \
+    do {                              \
+        sph_status s_ = (expr);       \
+        if (s_ != SPH_OK) return s_;  \
+    } while (0)
+
+// Makes room in the arena for a job of n dynamic and s static particles.
+static sph_status ensure_room(sph_server* sv, const Job& j)
+{
+    const uint64_t n = j.in.n, s = j.in.s, q = 2ull * j.in.n + 1, sq = (uint64_t)j.in.s + 1;
+    uint64_t need_n = sv->pa.needed_for(n), need_q = sv->qa.needed_for(q);
+    uint64_t need_s = sv->sa.needed_for(s), need_sq = sv->sqa.needed_for(sq);
+    if (need_n <= sv->pa.cap() && need_q <= sv->qa.cap() && need_s <= sv->sa.cap() && need_sq <= sv->sqa.cap())
+        return SPH_OK;
+    auto grown = [](uint64_t need, uint64_t cap) { return need <= cap ? cap : std::max(need, cap * 2); };
+    uint64_t cn = grown(need_n, sv->pa.cap()), cq = grown(need_q, sv->qa.cap());
+    uint64_t cs = grown(need_s, sv->sa.cap()), csq = grown(need_sq, sv->sqa.cap());
+    const uint64_t limit = (1ull << 31) - 64;
+    if (cn > limit || cq > limit || cs > limit || csq > limit) {
+        sph::set_last_error("arena index space exhausted");
+        return SPH_ERR_CAPACITY;
+    }
+    if (!sv->arena_ready) {
+        SRV_TRY(sv->arena.init_arena(sv->device, sv->stream, (uint32_t)cn, (uint32_t)cq, (uint32_t)cs, (uint32_t)csq,
+                                     sv->max_slots));
+        sv->arena_ready = true;
+    } else {
+        SRV_TRY(sv->arena.grow_arena((uint32_t)cn, (uint32_t)cq, (uint32_t)cs, (uint32_t)csq));
+    }
+    sv->pa.grow(cn);
+    sv->qa.grow(cq);
+    sv->sa.grow(cs);
+    sv->sqa.grow(csq);
+    return SPH_OK;
+}
+
+static SceneDesc desc_of(const Job& j)
+{
+    SceneDesc d = sph::scene_desc_for(j.in);
+    d.p_off = (uint32_t)j.p_off;
+    d.q_off = (uint32_t)j.q_off;
+    d.s_off = (uint32_t)j.s_off;
+    d.sq_off = (uint32_t)j.sq_off;
+    return d;
+}
+
+static sph_status admit(sph_server* sv, Job& j)
+{
+    SRV_TRY(ensure_room(sv, j));
+    const uint64_t n = j.in.n, q = 2ull * j.in.n + 1, s = j.in.s, sq = (uint64_t)j.in.s + 1;
+    bool ok = sv->pa.alloc(n, &j.p_off);
+    ok = ok && sv->qa.alloc(q, &j.q_off);
+    ok = ok && sv->sa.alloc(s, &j.s_off);
+    ok = ok && sv->sqa.alloc(sq, &j.sq_off);
+    if (!ok) {
+        sph::set_last_error("arena allocation failed after growth");
+        return SPH_ERR_CAPACITY;
+    }
+    SceneInput in = j.in;
+    in.pos = j.pos.data();
+    in.spos = j.spos.empty() ? nullptr : j.spos.data();
+    SRV_TRY(sv->arena.admit_scene(desc_of(j), in));
+    j.pos.clear();
+    j.pos.shrink_to_fit();
+    j.spos.clear();
+    j.spos.shrink_to_fit();
+    j.state = JobState::Active;
+    sv->used_bytes += j.bytes;
+    sv->active.push_back(j.id);
+    sv->dirty = true;
+    return SPH_OK;
+}
+
+static void release_ranges(sph_server* sv, Job& j)
+{
+    sv->pa.release(j.p_off, j.in.n);
+    sv->qa.release(j.q_off, 2ull * j.in.n + 1);
+    sv->sa.release(j.s_off, j.in.s);
+    sv->sqa.release(j.sq_off, (uint64_t)j.in.s + 1);
+    sv->used_bytes -= j.bytes;
+}
+
+extern "C" {
+
+SPH_API uint64_t sph_server_job_bytes(uint32_t n, uint32_t s) { return job_bytes(n, s); }
+
+SPH_API sph_status sph_server_create(sph_server** out, int device, uint64_t hbm_budget_bytes, uint32_t max_slots)
+{
+    if (!out || hbm_budget_bytes == 0 || max_slots == 0) return SPH_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int count = 0;
+    SRV_CUDA_TRY(cudaGetDeviceCount(&count));
+    if (device < 0 || device >= count) {
+        sph::set_last_error("no such CUDA device");
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    SRV_CUDA_TRY(cudaSetDevice(device));
+    sph_server* sv = new (std::nothrow) sph_server();
+    if (!sv) return SPH_ERR_OUT_OF_MEMORY;
+    cudaError_t e = cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete sv;
+        sph::set_last_error(cudaGetErrorString(e));
+        return SPH_ERR_CUDA;
+    }
+    sv->device = device;
+    sv->budget = hbm_budget_bytes;
+    sv->max_slots = max_slots;
+    *out = sv;
+    return SPH_OK;
+}
+
+SPH_API sph_status sph_server_destroy(sph_server* sv)
+{
+    if (!sv) return SPH_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(sv->device);
+    cudaStreamSynchronize(sv->stream);
+    sv->arena.release();
+    cudaStreamDestroy(sv->stream);
+    delete sv;
+    return SPH_OK;
+}
+
+SPH_API sph_status sph_server_submit(sph_server* sv, const sph_params* params, const float* dyn_pos, uint32_t n,
+                                     const float* static_pos, uint32_t s, float dt, uint32_t steps, uint64_t* job_id)
+{
+    if (!sv || !params || !job_id) return SPH_ERR_INVALID_ARGUMENT;
+    if (n == 0 || steps == 0 || !(dt > 0.f)) {
+        sph::set_last_error("a job needs particles, a positive dt and at least one step");
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    SceneInput in;
+    in.params = *params;
+    in.n = n;
+    in.s = s;
+    in.dt = dt;
+    in.pos = dyn_pos;
+    in.spos = static_pos;
+    SRV_TRY(sph::validate_scene(in));
+    auto j = std::make_unique<Job>();
+    j->bytes = job_bytes(n, s);
+    if (j->bytes > sv->budget) {
+        sph::set_last_error("job alone exceeds the HBM budget");
+        return SPH_ERR_BUDGET;
+    }
+    j->id = sv->next_id++;
+    j->in = in;
+    j->pos.assign(dyn_pos, dyn_pos + 3ull * n);
+    if (s) j->spos.assign(static_pos, static_pos + 3ull * s);
+    j->in.pos = nullptr;
+    j->in.spos = nullptr;
+    j->steps = steps;
+    j->gas = params->gas_constant;
+    j->rho0 = params->rest_density;
+    *job_id = j->id;
+    sv->queue.push_back(j->id);
+    sv->jobs.emplace(j->id, std::move(j));
+    return SPH_OK;
+}
+
+SPH_API sph_status sph_server_poll(sph_server* sv, uint32_t chunk_steps, uint32_t* active_out, uint32_t* queued_out)
+{
+    if (!sv || chunk_steps == 0) return SPH_ERR_INVALID_ARGUMENT;
+    SRV_CUDA_TRY(cudaSetDevice(sv->device));
+    // admit in arrival order; later jobs may pass one that does not fit
+    for (auto it = sv->queue.begin(); it != sv->queue.end() && sv->active.size() < sv->max_slots;) {
+        Job& j = *sv->jobs[*it];
+        if (sv->used_bytes + j.bytes <= sv->budget) {
+            SRV_TRY(admit(sv, j));
+            it = sv->queue.erase(it);
+        } else {
+            ++it;
+        }
+    }
+    if (!sv->active.empty()) {
+        if (sv->dirty) {
+            std::vector<SceneDesc> descs;
+            for (uint64_t id : sv->active) descs.push_back(desc_of(*sv->jobs[id]));
+            SRV_TRY(sv->arena.set_active(descs));
+            sv->dirty = false;
+        }
+        uint32_t steps = chunk_steps;
+        for (uint64_t id : sv->active) {
+            const Job& j = *sv->jobs[id];
+            steps = std::min(steps, j.steps - j.done);
+        }
+        SRV_TRY(sv->arena.enqueue_steps(steps, sph::StepMode::Persistent, false, false));
+        SRV_CUDA_TRY(cudaStreamSynchronize(sv->stream));
+        SRV_TRY(sv->arena.check_device_error());
+        std::vector<uint64_t> still;
+        for (size_t k = 0; k < sv->active.size(); ++k) {
+            Job& j = *sv->jobs[sv->active[k]];
+            j.done += steps;
+            if (j.done >= j.steps) {
+                j.result.resize(j.in.n);
+                SRV_TRY(sv->arena.read_scene((uint32_t)k, j.result.data(), nullptr));
+                j.state = JobState::Finished;
+                release_ranges(sv, j);
+                sv->dirty = true;
+            } else {
+                still.push_back(j.id);
+            }
+        }
+        sv->active.swap(still);
+    }
+    if (active_out) *active_out = (uint32_t)sv->active.size();
+    if (queued_out) *queued_out = (uint32_t)sv->queue.size();
+    return SPH_OK;
+}
+
+SPH_API sph_status sph_server_result(sph_server* sv, uint64_t job_id, sph_dynamic_particle* out, float* density)
+{
+    if (!sv) return SPH_ERR_INVALID_ARGUMENT;
+    auto it = sv->jobs.find(job_id);
+    if (it == sv->jobs.end() || it->second->state != JobState::Finished) {
+        sph::set_last_error("job unknown or not finished");
+        return SPH_ERR_NOT_FOUND;
+    }
+    Job& j = *it->second;
+    if (out) std::copy(j.result.begin(), j.result.end(), out);
+    if (density)
+        for (uint32_t i = 0; i < j.in.n; ++i) density[i] = j.result[i].pressure / j.gas + j.rho0;
+    sv->jobs.erase(it);
+    return SPH_OK;
+}
+
+}  // extern "C"

@@ -47,6 +47,8 @@ enum class StepMode { Staged = 0, Persistent = 1 };
 void set_last_error(const std::string& s);
 const char* last_error();
 sph_status validate_scene(const SceneInput& in);
+// Physics constants and sizes of a scene (offsets left zero).
+SceneDesc scene_desc_for(const SceneInput& in);
 
 class StepState {
 public:
@@ -73,6 +75,21 @@ public:
     sph_status persistent_grid(uint32_t* grid);
     // Outputs of the initial sort of scene 0 (see sph_cell_sort).
     sph_status read_sort(uint32_t* keys, uint32_t* counts, uint32_t* starts, uint32_t* order);
+
+    // ---- arena mode (server): fixed-capacity arrays, each scene occupies
+    // ranges of the slot / bucket / static index spaces chosen by the caller.
+    sph_status init_arena(int device, cudaStream_t stream, uint32_t cap_n, uint32_t cap_q, uint32_t cap_s,
+                          uint32_t cap_sq, uint32_t max_scenes);
+    // Grows every array to at least the given capacities, keeping contents.
+    sph_status grow_arena(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s, uint32_t cap_sq);
+    // Uploads one scene into its ranges (d's offsets) and sorts it alone.
+    sph_status admit_scene(const SceneDesc& d, const SceneInput& in);
+    // Replaces the set of scenes the step advances (table, tiles, scan range).
+    sph_status set_active(const std::vector<SceneDesc>& descs);
+    uint32_t cap_n() const { return cap_n_; }
+    uint32_t cap_q() const { return cap_q_; }
+    uint32_t cap_s() const { return cap_s_; }
+    uint32_t cap_sq() const { return cap_sq_; }
 
     const float* stage_ms() const { return stage_ms_; }
     void set_persistent_ctas(uint32_t c) { persistent_ctas_ = c; }
@@ -103,7 +120,9 @@ public:
 private:
     sph_status enqueue_load(const float4* src, bool statics);
     sph_status enqueue_sort(bool statics);
-    sph_status enqueue_scan(uint32_t* out, uint32_t len);
+    sph_status enqueue_scan(uint32_t* cnt, uint32_t* out, uint32_t len);
+    sph_status alloc_arrays(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s, uint32_t cap_sq, uint32_t cap_t,
+                            uint32_t max_scenes, uint32_t max_tiles);
     sph_status enqueue_step_staged(bool record_accel, bool timed);
     sph_status enqueue_step_persistent();
     sph_status ensure_events();
@@ -116,6 +135,10 @@ private:
     cudaEvent_t events_[6] = {};
     float stage_ms_[5] = {};
     uint32_t persistent_ctas_ = 0;
+    uint32_t cap_n_ = 0, cap_q_ = 0, cap_s_ = 0, cap_sq_ = 0, cap_t_ = 0, max_scenes_ = 0, max_tiles_ = 0;
+    std::vector<uint32_t> tile_first_;     // first tile of each scene
+    Tile* d_tmp_tiles_ = nullptr;          // tiles of a scene being admitted
+    SceneDesc* d_tmp_scene_ = nullptr;     // its dynamic and static views
 };
 
 }  // namespace sph

@@ -181,11 +181,12 @@ void StepState::release()
 {
     if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
     void* ptrs[] = {d_scenes, d_sscenes, d_tiles, d_stiles, pos, vel, pos_tmp, vel_tmp, key, arrival, perm, count,
-                    start, scan_status, scan_ticket, err, bar, spos, sstart, tris, accel, accel_io, staging};
+                    start, scan_status, scan_ticket, err, bar, spos, sstart, tris, accel, accel_io, staging,
+                    d_tmp_tiles_, d_tmp_scene_};
     for (void* p : ptrs)
         if (p) cudaFree(p);
-    d_scenes = d_sscenes = nullptr;
-    d_tiles = d_stiles = nullptr;
+    d_scenes = d_sscenes = d_tmp_scene_ = nullptr;
+    d_tiles = d_stiles = d_tmp_tiles_ = nullptr;
     pos = vel = pos_tmp = vel_tmp = spos = accel = accel_io = nullptr;
     staging = nullptr;
     key = arrival = perm = count = start = scan_ticket = err = bar = sstart = nullptr;
@@ -197,8 +198,10 @@ void StepState::release()
     scenes.clear();
     tiles.clear();
     stiles.clear();
+    tile_first_.clear();
     total_n = total_s = total_t = 0;
     scan_len = sscan_len = 0;
+    cap_n_ = cap_q_ = cap_s_ = cap_sq_ = cap_t_ = max_scenes_ = max_tiles_ = 0;
 }
 
 static SceneDesc make_scene_desc(const sph_params& p, float dt)
@@ -216,6 +219,30 @@ static SceneDesc make_scene_desc(const sph_params& p, float dt)
     d.kc = kernel_constant(d.h);
     d.self_density = self_density(d.mass, d.h, d.kc);
     d.dt = dt;
+    return d;
+}
+
+SceneDesc scene_desc_for(const SceneInput& in)
+{
+    SceneDesc d = make_scene_desc(in.params, in.dt);
+    d.n = in.n;
+    d.buckets = in.buckets ? in.buckets : 2u * in.n;
+    d.s = in.s;
+    d.t = in.t;
+    d.fm_b = make_fastmod(d.buckets);
+    d.fm_s = make_fastmod(in.s);
+    return d;
+}
+
+static SceneDesc static_view(SceneDesc d)
+{
+    // the same scene with the static index spaces in the dynamic fields, so
+    // the sort kernels serve both particle kinds
+    d.p_off = d.s_off;
+    d.n = d.s;
+    d.q_off = d.sq_off;
+    d.buckets = d.s;
+    d.fm_b = d.fm_s;
     return d;
 }
 
@@ -240,6 +267,78 @@ sph_status validate_scene(const SceneInput& in)
     return SPH_OK;
 }
 
+static uint32_t tiles_for(uint32_t n) { return (n + kTileThreads - 1) / kTileThreads; }
+
+// Allocates every device array for the given capacities (all zero-filled
+// where the algorithm needs zeros: bucket counters, scan status, errors).
+sph_status StepState::alloc_arrays(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s, uint32_t cap_sq, uint32_t cap_t,
+                                   uint32_t max_scenes, uint32_t max_tiles)
+{
+    cap_n_ = cap_n;
+    cap_q_ = cap_q;
+    cap_s_ = cap_s;
+    cap_sq_ = cap_sq;
+    cap_t_ = cap_t;
+    max_scenes_ = std::max<uint32_t>(1, max_scenes);
+    max_tiles_ = std::max<uint32_t>(1, max_tiles);
+    const uint32_t work_n = std::max(cap_n, cap_s);
+    const uint32_t cnt_len = std::max(cap_q, cap_sq) + 1u;
+    const uint32_t scan_tiles_max = (cnt_len + kScanTile - 1) / kScanTile;
+    sph_status st;
+#define ALLOC(ptr, cnt) if ((st = dev_alloc(&(ptr), (cnt))) != SPH_OK) return st
+    ALLOC(d_scenes, max_scenes_);
+    ALLOC(d_sscenes, max_scenes_);
+    ALLOC(d_tiles, max_tiles_);
+    ALLOC(d_stiles, max_tiles_);
+    ALLOC(d_tmp_tiles_, tiles_for(work_n) + 1);
+    ALLOC(d_tmp_scene_, 2);
+    ALLOC(pos, cap_n);
+    ALLOC(vel, cap_n);
+    ALLOC(pos_tmp, work_n);
+    ALLOC(vel_tmp, work_n);
+    ALLOC(key, work_n);
+    ALLOC(arrival, work_n);
+    ALLOC(perm, work_n);
+    ALLOC(count, cnt_len);
+    ALLOC(start, cap_q + 1ull);
+    ALLOC(scan_status, scan_tiles_max);
+    ALLOC(scan_ticket, 1);
+    ALLOC(err, 1);
+    ALLOC(bar, 2);
+    ALLOC(spos, cap_s);
+    ALLOC(sstart, cap_sq + 1ull);
+    ALLOC(tris, 9ull * cap_t);
+    ALLOC(staging, 2ull * work_n);
+#undef ALLOC
+    CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(uint32_t) * cnt_len, stream_));
+    CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(uint32_t), stream_));
+    CUDA_TRY(cudaMemsetAsync(bar, 0, 2 * sizeof(uint32_t), stream_));
+    CUDA_TRY(cudaMemsetAsync(scan_status, 0, sizeof(unsigned long long) * scan_tiles_max, stream_));
+    CUDA_TRY(cudaStreamSynchronize(stream_));
+    return SPH_OK;
+}
+
+// Host positions (and velocities) of one scene -> staging as float4 pairs.
+static sph_status upload_particles(cudaStream_t stream, float4* staging, uint32_t off, const float* p, const float* v,
+                                   uint32_t n)
+{
+    if (!n) return SPH_OK;
+    std::vector<float> hbuf(8ull * n, 0.f);
+    for (uint32_t i = 0; i < n; ++i) {
+        hbuf[8ull * i + 0] = p[3ull * i + 0];
+        hbuf[8ull * i + 1] = p[3ull * i + 1];
+        hbuf[8ull * i + 2] = p[3ull * i + 2];
+        if (v) {
+            hbuf[8ull * i + 4] = v[3ull * i + 0];
+            hbuf[8ull * i + 5] = v[3ull * i + 1];
+            hbuf[8ull * i + 6] = v[3ull * i + 2];
+        }
+    }
+    CUDA_TRY(cudaMemcpyAsync(staging + 2ull * off, hbuf.data(), sizeof(float) * hbuf.size(), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    return SPH_OK;
+}
+
 sph_status StepState::build(int device, cudaStream_t stream, const std::vector<SceneInput>& inputs)
 {
     release();
@@ -250,19 +349,14 @@ sph_status StepState::build(int device, cudaStream_t stream, const std::vector<S
         const SceneInput& in = inputs[k];
         sph_status st = validate_scene(in);
         if (st != SPH_OK) return st;
-        SceneDesc d = make_scene_desc(in.params, in.dt);
+        SceneDesc d = scene_desc_for(in);
         d.p_off = (uint32_t)p_off;
-        d.n = in.n;
         d.q_off = (uint32_t)q_off;
-        d.buckets = in.buckets ? in.buckets : 2u * in.n;
         d.s_off = (uint32_t)s_off;
-        d.s = in.s;
         d.sq_off = (uint32_t)sq_off;
         d.t_off = (uint32_t)t_off;
-        d.t = in.t;
-        d.fm_b = make_fastmod(d.buckets);
-        d.fm_s = make_fastmod(in.s);
         scenes.push_back(d);
+        tile_first_.push_back((uint32_t)tiles.size());
         for (uint32_t b = 0; b < in.n; b += kTileThreads)
             tiles.push_back(Tile{(uint32_t)k, (uint32_t)(p_off + b), (uint32_t)(p_off + std::min<uint64_t>(b + kTileThreads, in.n)), 0});
         for (uint32_t b = 0; b < in.s; b += kTileThreads)
@@ -272,58 +366,22 @@ sph_status StepState::build(int device, cudaStream_t stream, const std::vector<S
         s_off += in.s;
         sq_off += in.s;
         t_off += in.t;
-    }
-    if (p_off > kMaxParticles || s_off > kMaxParticles || q_off >= (1ull << 31)) {
-        set_last_error("total particle count exceeds 2^30");
-        return SPH_ERR_CAPACITY;
+        if (p_off > kMaxParticles || s_off > kMaxParticles || q_off >= (1ull << 31)) {
+            set_last_error("total particle or bucket count exceeds the 32-bit index space");
+            return SPH_ERR_CAPACITY;
+        }
     }
     total_n = (uint32_t)p_off;
     total_s = (uint32_t)s_off;
     total_t = (uint32_t)t_off;
     scan_len = (uint32_t)q_off + 1u;
     sscan_len = (uint32_t)sq_off + 1u;
-    const uint32_t scan_tiles_max = (std::max(scan_len, sscan_len) + kScanTile - 1) / kScanTile;
-    const uint32_t work_n = std::max(total_n, total_s);
-
-    sph_status st;
-#define ALLOC(ptr, cnt) if ((st = dev_alloc(&(ptr), (cnt))) != SPH_OK) return st
-    ALLOC(d_scenes, scenes.size());
-    ALLOC(d_sscenes, scenes.size());
-    ALLOC(d_tiles, tiles.size());
-    ALLOC(d_stiles, stiles.size());
-    ALLOC(pos, total_n);
-    ALLOC(vel, total_n);
-    ALLOC(pos_tmp, work_n);
-    ALLOC(vel_tmp, work_n);
-    ALLOC(key, work_n);
-    ALLOC(arrival, work_n);
-    ALLOC(perm, work_n);
-    ALLOC(count, std::max(scan_len, sscan_len));
-    ALLOC(start, scan_len);
-    ALLOC(scan_status, scan_tiles_max);
-    ALLOC(scan_ticket, 1);
-    ALLOC(err, 1);
-    ALLOC(bar, 2);
-    ALLOC(spos, total_s);
-    ALLOC(sstart, sscan_len);
-    ALLOC(tris, 9ull * total_t);
-    ALLOC(staging, 2ull * std::max(total_n, total_s));
-#undef ALLOC
-    CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(uint32_t) * std::max(scan_len, sscan_len), stream_));
-    CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(uint32_t), stream_));
-    CUDA_TRY(cudaMemsetAsync(bar, 0, 2 * sizeof(uint32_t), stream_));
-    CUDA_TRY(cudaMemsetAsync(scan_status, 0, sizeof(unsigned long long) * scan_tiles_max, stream_));
+    sph_status st = alloc_arrays(total_n, (uint32_t)q_off, total_s, (uint32_t)sq_off, total_t, (uint32_t)scenes.size(),
+                                 (uint32_t)std::max(tiles.size(), stiles.size()));
+    if (st != SPH_OK) return st;
+    std::vector<SceneDesc> sview;
+    for (const auto& d : scenes) sview.push_back(static_view(d));
     CUDA_TRY(cudaMemcpyAsync(d_scenes, scenes.data(), sizeof(SceneDesc) * scenes.size(), cudaMemcpyHostToDevice, stream_));
-    // static view: the same scenes with the static index spaces in the
-    // dynamic fields, so the sort kernels serve both particle kinds
-    std::vector<SceneDesc> sview = scenes;
-    for (auto& d : sview) {
-        d.p_off = d.s_off;
-        d.n = d.s;
-        d.q_off = d.sq_off;
-        d.buckets = d.s;
-        d.fm_b = d.fm_s;
-    }
     CUDA_TRY(cudaMemcpyAsync(d_sscenes, sview.data(), sizeof(SceneDesc) * sview.size(), cudaMemcpyHostToDevice, stream_));
     if (!tiles.empty())
         CUDA_TRY(cudaMemcpyAsync(d_tiles, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice, stream_));
@@ -331,46 +389,22 @@ sph_status StepState::build(int device, cudaStream_t stream, const std::vector<S
         CUDA_TRY(cudaMemcpyAsync(d_stiles, stiles.data(), sizeof(Tile) * stiles.size(), cudaMemcpyHostToDevice, stream_));
     CUDA_TRY(cudaStreamSynchronize(stream_));
 
-    // upload every scene, then sort statics and dynamics
-    std::vector<float> hbuf;
+    // statics of every scene first (staging is their scratch), then dynamics
     for (size_t k = 0; k < inputs.size(); ++k) {
-        const SceneInput& in = inputs[k];
-        const SceneDesc& d = scenes[k];
-        if (in.s) {
-            hbuf.assign(8ull * in.s, 0.f);
-            for (uint32_t i = 0; i < in.s; ++i) {
-                hbuf[8ull * i + 0] = in.spos[3ull * i + 0];
-                hbuf[8ull * i + 1] = in.spos[3ull * i + 1];
-                hbuf[8ull * i + 2] = in.spos[3ull * i + 2];
-            }
-            CUDA_TRY(cudaMemcpyAsync(staging + 2ull * d.s_off, hbuf.data(), sizeof(float) * hbuf.size(), cudaMemcpyHostToDevice, stream_));
-            CUDA_TRY(cudaStreamSynchronize(stream_));
-        }
-        if (in.t)
-            CUDA_TRY(cudaMemcpyAsync(tris + 9ull * d.t_off, in.tris, sizeof(float) * 9ull * in.t, cudaMemcpyHostToDevice, stream_));
+        if ((st = upload_particles(stream_, staging, scenes[k].s_off, inputs[k].spos, nullptr, inputs[k].s)) != SPH_OK)
+            return st;
+        if (inputs[k].t)
+            CUDA_TRY(cudaMemcpyAsync(tris + 9ull * scenes[k].t_off, inputs[k].tris, sizeof(float) * 9ull * inputs[k].t,
+                                     cudaMemcpyHostToDevice, stream_));
     }
     if (total_s) {
         if ((st = enqueue_load(staging, /*statics=*/true)) != SPH_OK) return st;
         if ((st = enqueue_sort(/*statics=*/true)) != SPH_OK) return st;
-    }
-    for (size_t k = 0; k < inputs.size(); ++k) {
-        const SceneInput& in = inputs[k];
-        const SceneDesc& d = scenes[k];
-        if (!in.n) continue;
-        hbuf.assign(8ull * in.n, 0.f);
-        for (uint32_t i = 0; i < in.n; ++i) {
-            hbuf[8ull * i + 0] = in.pos[3ull * i + 0];
-            hbuf[8ull * i + 1] = in.pos[3ull * i + 1];
-            hbuf[8ull * i + 2] = in.pos[3ull * i + 2];
-            if (in.vel) {
-                hbuf[8ull * i + 4] = in.vel[3ull * i + 0];
-                hbuf[8ull * i + 5] = in.vel[3ull * i + 1];
-                hbuf[8ull * i + 6] = in.vel[3ull * i + 2];
-            }
-        }
-        CUDA_TRY(cudaMemcpyAsync(staging + 2ull * d.p_off, hbuf.data(), sizeof(float) * hbuf.size(), cudaMemcpyHostToDevice, stream_));
         CUDA_TRY(cudaStreamSynchronize(stream_));
     }
+    for (size_t k = 0; k < inputs.size(); ++k)
+        if ((st = upload_particles(stream_, staging, scenes[k].p_off, inputs[k].pos, inputs[k].vel, inputs[k].n)) != SPH_OK)
+            return st;
     if (total_n) {
         if ((st = enqueue_load(staging, false)) != SPH_OK) return st;
         if ((st = enqueue_sort(false)) != SPH_OK) return st;
@@ -378,6 +412,166 @@ sph_status StepState::build(int device, cudaStream_t stream, const std::vector<S
     CUDA_TRY(cudaStreamSynchronize(stream_));
     return check_device_error();
 }
+
+// ---- arena mode ---------------------------------------------------------------
+
+sph_status StepState::init_arena(int device, cudaStream_t stream, uint32_t cap_n, uint32_t cap_q, uint32_t cap_s,
+                                 uint32_t cap_sq, uint32_t max_scenes)
+{
+    release();
+    device_ = device;
+    stream_ = stream;
+    return alloc_arrays(cap_n, cap_q, cap_s, cap_sq, 0, max_scenes, tiles_for(cap_n) + max_scenes);
+}
+
+template <typename T>
+static sph_status grow_one(T** p, size_t old_count, size_t new_count, bool zero_tail, cudaStream_t stream)
+{
+    T* q = nullptr;
+    sph_status st = dev_alloc(&q, new_count);
+    if (st != SPH_OK) return st;
+    if (*p && old_count)
+        CUDA_TRY(cudaMemcpyAsync(q, *p, sizeof(T) * old_count, cudaMemcpyDeviceToDevice, stream));
+    if (zero_tail && new_count > old_count)
+        CUDA_TRY(cudaMemsetAsync(q + old_count, 0, sizeof(T) * (new_count - old_count), stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    if (*p) cudaFree(*p);
+    *p = q;
+    return SPH_OK;
+}
+
+sph_status StepState::grow_arena(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s, uint32_t cap_sq)
+{
+    cap_n = std::max(cap_n, cap_n_);
+    cap_q = std::max(cap_q, cap_q_);
+    cap_s = std::max(cap_s, cap_s_);
+    cap_sq = std::max(cap_sq, cap_sq_);
+    if (cap_n == cap_n_ && cap_q == cap_q_ && cap_s == cap_s_ && cap_sq == cap_sq_) return SPH_OK;
+    if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+    const size_t old_work = std::max(cap_n_, cap_s_), new_work = std::max(cap_n, cap_s);
+    const size_t old_cnt = std::max(cap_q_, cap_sq_) + 1ull, new_cnt = std::max(cap_q, cap_sq) + 1ull;
+    const size_t new_scan_tiles = (new_cnt + kScanTile - 1) / kScanTile;
+    sph_status st;
+#define GROW(ptr, o, nw, z) if ((st = grow_one(&(ptr), (o), (nw), (z), stream_)) != SPH_OK) return st
+    GROW(pos, cap_n_, cap_n, false);
+    GROW(vel, cap_n_, cap_n, false);
+    GROW(pos_tmp, old_work, new_work, false);
+    GROW(vel_tmp, old_work, new_work, false);
+    GROW(key, old_work, new_work, false);
+    GROW(arrival, old_work, new_work, false);
+    GROW(perm, old_work, new_work, false);
+    GROW(staging, 2 * old_work, 2 * new_work, false);
+    GROW(count, old_cnt, new_cnt, true);
+    GROW(start, cap_q_ + 1ull, cap_q + 1ull, false);
+    GROW(spos, cap_s_, cap_s, false);
+    GROW(sstart, cap_sq_ + 1ull, cap_sq + 1ull, false);
+    GROW(scan_status, 0, new_scan_tiles, true);
+    GROW(d_tmp_tiles_, 0, tiles_for((uint32_t)new_work) + 1, false);
+    GROW(d_tiles, 0, tiles_for(cap_n) + max_scenes_, false);
+    GROW(d_stiles, 0, tiles_for(cap_n) + max_scenes_, false);
+#undef GROW
+    if (accel) { cudaFree(accel); accel = nullptr; }
+    if (accel_io) { cudaFree(accel_io); accel_io = nullptr; }
+    max_tiles_ = tiles_for(cap_n) + max_scenes_;
+    cap_n_ = cap_n;
+    cap_q_ = cap_q;
+    cap_s_ = cap_s;
+    cap_sq_ = cap_sq;
+    return set_active(scenes);
+}
+
+// Sorts one scene alone: its own tiles and one-entry scene tables, and scans
+// over its own bucket ranges only, so every other scene's table is untouched
+// (a sub-range scan yields local starts; the per-scene delta absorbs that).
+sph_status StepState::admit_scene(const SceneDesc& d, const SceneInput& in)
+{
+    if (d.p_off + (uint64_t)d.n > cap_n_ || d.q_off + (uint64_t)d.buckets + 1 > cap_q_ + 1ull ||
+        d.s_off + (uint64_t)d.s > cap_s_ || d.sq_off + (uint64_t)d.s + 1 > cap_sq_ + 1ull) {
+        set_last_error("scene ranges exceed the arena");
+        return SPH_ERR_CAPACITY;
+    }
+    if ((d.q_off & 3u) || (d.sq_off & 3u)) {
+        set_last_error("bucket ranges must start on a multiple of 4");
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    SceneDesc views[2] = {d, static_view(d)};
+    CUDA_TRY(cudaMemcpyAsync(d_tmp_scene_, views, sizeof(views), cudaMemcpyHostToDevice, stream_));
+    std::vector<Tile> tl;
+    sph_status st;
+    for (int kind = 1; kind >= 0; --kind) {            // statics first, then dynamics
+        const SceneDesc& v = views[kind];
+        if (!v.n) continue;
+        tl.clear();
+        for (uint32_t b = 0; b < v.n; b += kTileThreads)
+            tl.push_back(Tile{(uint32_t)kind, v.p_off + b, v.p_off + std::min<uint32_t>(b + kTileThreads, v.n), 0});
+        CUDA_TRY(cudaMemcpyAsync(d_tmp_tiles_, tl.data(), sizeof(Tile) * tl.size(), cudaMemcpyHostToDevice, stream_));
+        if (kind == 1) {
+            if ((st = upload_particles(stream_, staging, v.p_off, in.spos, nullptr, v.n)) != SPH_OK) return st;
+        } else {
+            if ((st = upload_particles(stream_, staging, v.p_off, in.pos, in.vel, v.n)) != SPH_OK) return st;
+        }
+        const unsigned nt = (unsigned)tl.size();
+        k_load<<<nt, kTileThreads, 0, stream_>>>(d_tmp_tiles_, d_tmp_scene_, staging, pos_tmp, vel_tmp);
+        CUDA_TRY(cudaGetLastError());
+        SortArgs a{};
+        a.tiles = d_tmp_tiles_;
+        a.scenes = d_tmp_scene_;
+        a.pos_src = pos_tmp;
+        a.vel_src = vel_tmp;
+        a.pos_dst = kind ? spos : pos;
+        a.vel_dst = kind ? staging : vel;
+        a.key = key;
+        a.arrival = arrival;
+        a.perm = perm;
+        a.count = count;
+        a.start = kind ? sstart : start;
+        a.err = err;
+        k_hash_count<<<nt, kTileThreads, 0, stream_>>>(a);
+        CUDA_TRY(cudaGetLastError());
+        if ((st = enqueue_scan(count + v.q_off, a.start + v.q_off, v.buckets + 1u)) != SPH_OK) return st;
+        k_scatter<<<nt, kTileThreads, 0, stream_>>>(a);
+        CUDA_TRY(cudaGetLastError());
+        k_gather<<<nt, kTileThreads, 0, stream_>>>(a);
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaStreamSynchronize(stream_));
+    }
+    return check_device_error();
+}
+
+sph_status StepState::set_active(const std::vector<SceneDesc>& descs)
+{
+    if (descs.size() > max_scenes_) {
+        set_last_error("more scenes than the arena's slots");
+        return SPH_ERR_CAPACITY;
+    }
+    if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+    scenes = descs;
+    tiles.clear();
+    tile_first_.clear();
+    uint64_t qmax = 0, tn = 0;
+    for (size_t k = 0; k < scenes.size(); ++k) {
+        const SceneDesc& d = scenes[k];
+        tile_first_.push_back((uint32_t)tiles.size());
+        for (uint32_t b = 0; b < d.n; b += kTileThreads)
+            tiles.push_back(Tile{(uint32_t)k, d.p_off + b, d.p_off + std::min<uint32_t>(b + kTileThreads, d.n), 0});
+        qmax = std::max<uint64_t>(qmax, (uint64_t)d.q_off + d.buckets);
+        tn += d.n;
+    }
+    if (tiles.size() > max_tiles_) {
+        set_last_error("tile table overflow");
+        return SPH_ERR_CAPACITY;
+    }
+    total_n = (uint32_t)tn;
+    scan_len = (uint32_t)qmax + 1u;
+    if (!scenes.empty())
+        CUDA_TRY(cudaMemcpyAsync(d_scenes, scenes.data(), sizeof(SceneDesc) * scenes.size(), cudaMemcpyHostToDevice, stream_));
+    if (!tiles.empty())
+        CUDA_TRY(cudaMemcpyAsync(d_tiles, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice, stream_));
+    CUDA_TRY(cudaStreamSynchronize(stream_));
+    return SPH_OK;
+}
+
+// ---- launches -------------------------------------------------------------------
 
 sph_status StepState::enqueue_load(const float4* src, bool statics)
 {
@@ -418,7 +612,7 @@ sph_status StepState::enqueue_sort(bool statics)
     const unsigned nt = (unsigned)tl.size();
     k_hash_count<<<nt, kTileThreads, 0, stream_>>>(a);
     CUDA_TRY(cudaGetLastError());
-    sph_status st = enqueue_scan(a.start, len);
+    sph_status st = enqueue_scan(count, a.start, len);
     if (st != SPH_OK) return st;
     k_scatter<<<nt, kTileThreads, 0, stream_>>>(a);
     CUDA_TRY(cudaGetLastError());
@@ -427,12 +621,12 @@ sph_status StepState::enqueue_sort(bool statics)
     return SPH_OK;
 }
 
-sph_status StepState::enqueue_scan(uint32_t* out, uint32_t len)
+sph_status StepState::enqueue_scan(uint32_t* cnt, uint32_t* out, uint32_t len)
 {
     const uint32_t tiles_n = (len + kScanTile - 1) / kScanTile;
     CUDA_TRY(cudaMemsetAsync(scan_status, 0, sizeof(unsigned long long) * tiles_n, stream_));
     CUDA_TRY(cudaMemsetAsync(scan_ticket, 0, sizeof(uint32_t), stream_));
-    k_scan<<<tiles_n, kScanThreads, 0, stream_>>>(count, out, len, scan_status, scan_ticket, err);
+    k_scan<<<tiles_n, kScanThreads, 0, stream_>>>(cnt, out, len, scan_status, scan_ticket, err);
     CUDA_TRY(cudaGetLastError());
     return SPH_OK;
 }
@@ -490,7 +684,7 @@ sph_status StepState::enqueue_step_staged(bool record_accel, bool timed)
         k_force<false><<<nt, kTileThreads, 0, stream_>>>(a);
     CUDA_TRY(cudaGetLastError());
     if (timed) CUDA_TRY(cudaEventRecord(events_[2], stream_));
-    sph_status st = enqueue_scan(start, scan_len);
+    sph_status st = enqueue_scan(count, start, scan_len);
     if (st != SPH_OK) return st;
     if (timed) CUDA_TRY(cudaEventRecord(events_[3], stream_));
     k_scatter<<<nt, kTileThreads, 0, stream_>>>(s);
@@ -621,8 +815,11 @@ sph_status StepState::read_scene(uint32_t scene, sph_dynamic_particle* out, floa
         sph_status st = dev_alloc(&accel_io, total_n);
         if (st != SPH_OK) return st;
     }
-    k_unsort<<<(unsigned)tiles.size(), kTileThreads, 0, stream_>>>(d_tiles, d_scenes, pos, vel, staging,
-                                                                  accel_out ? accel : nullptr, accel_io);
+    const uint32_t t0 = tile_first_[scene];
+    const uint32_t t1 = scene + 1 < tile_first_.size() ? tile_first_[scene + 1] : (uint32_t)tiles.size();
+    if (t1 > t0)
+        k_unsort<<<t1 - t0, kTileThreads, 0, stream_>>>(d_tiles + t0, d_scenes, pos, vel, staging,
+                                                        accel_out ? accel : nullptr, accel_io);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaMemcpyAsync(out, staging + 2ull * d.p_off, sizeof(sph_dynamic_particle) * d.n, cudaMemcpyDeviceToHost, stream_));
     if (accel_out) {

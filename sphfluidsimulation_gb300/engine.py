@@ -230,3 +230,62 @@ class Batch:
         thr = C.c_uint32()
         check(self.lib.sph_batch_info(self.h, C.byref(tot), C.byref(grid), C.byref(thr)), "sph_batch_info")
         return tot.value, grid.value, thr.value
+
+
+class Server:
+    """Continuous-batching server: jobs admitted under an HBM budget, resident
+    on the device, advanced together; results returned per job."""
+
+    def __init__(self, budget_bytes: int, max_slots: int = 64, device: int = 0):
+        self.lib = _lib.load()
+        h = C.c_void_p()
+        check(self.lib.sph_server_create(C.byref(h), int(device), int(budget_bytes), int(max_slots)),
+              "sph_server_create")
+        self.h = h
+        self.sizes = {}
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.sph_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def job_bytes(n: int, s: int) -> int:
+        return int(_lib.load().sph_server_job_bytes(int(n), int(s)))
+
+    def submit(self, scene, steps: Optional[int] = None) -> int:
+        dyn = _f32(scene.dyn_pos, 3)
+        st = _f32(scene.static_pos, 3)
+        p = make_params(scene.params)
+        jid = C.c_uint64()
+        n = 0 if dyn is None else dyn.shape[0]
+        check(self.lib.sph_server_submit(self.h, C.byref(p), _fptr(dyn), n, _fptr(st),
+                                         0 if st is None else st.shape[0], float(scene.dt),
+                                         int(scene.steps if steps is None else steps), C.byref(jid)),
+              "sph_server_submit")
+        self.sizes[jid.value] = n
+        return jid.value
+
+    def poll(self, chunk_steps: int = 50):
+        a = C.c_uint32()
+        q = C.c_uint32()
+        check(self.lib.sph_server_poll(self.h, int(chunk_steps), C.byref(a), C.byref(q)), "sph_server_poll")
+        return a.value, q.value
+
+    def result(self, job_id: int):
+        """(particles, density) of a finished job, or None while it runs."""
+        n = self.sizes[job_id]
+        out = np.zeros(n, DYN_DTYPE)
+        dens = np.zeros(n, np.float32)
+        st = self.lib.sph_server_result(self.h, C.c_uint64(job_id), out.ctypes.data_as(C.c_void_p), _fptr(dens))
+        if st == 8:
+            return None
+        check(st, "sph_server_result")
+        del self.sizes[job_id]
+        return out, dens

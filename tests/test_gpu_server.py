@@ -1,0 +1,82 @@
+"""Served form: jobs of different sizes and horizons admitted under an HBM
+budget, advanced together; each result equals the same job run alone on the
+plain engine, bit for bit (and so within any tolerance)."""
+import numpy as np
+import pytest
+
+from sphfluidsimulation_gb300 import scenes
+from sphfluidsimulation_gb300._lib import SphError
+from sphfluidsimulation_gb300.engine import Server, SimulationEngineCUDA
+
+pytestmark = pytest.mark.gpu
+
+
+def job(n, steps, seed):
+    j = scenes.Job(job_id=seed, arrival_s=0.0, n=n, steps=steps, seed=seed)
+    return scenes.job_scene(j)
+
+
+def alone(sc):
+    e = SimulationEngineCUDA()
+    e.initialize(sc)
+    e.update(sc.dt, sc.steps)
+    return e.read_dynamic()
+
+
+def test_results_alone_equal_in_the_mix():
+    specs = [(3000, 17, 1), (500, 40, 2), (9000, 9, 3), (1200, 33, 4), (2500, 25, 5), (700, 3, 6)]
+    scs = [job(n, st, sd) for n, st, sd in specs]
+    srv = Server(budget_bytes=1 << 30, max_slots=4)
+    ids = [srv.submit(sc) for sc in scs[:4]]
+    # more work arrives while the first jobs are on the GPU
+    a, q = srv.poll(5)
+    ids += [srv.submit(sc) for sc in scs[4:]]
+    done = {}
+    for _ in range(200):
+        a, q = srv.poll(7)
+        for jid in ids:
+            if jid not in done:
+                r = srv.result(jid)
+                if r is not None:
+                    done[jid] = r
+        if len(done) == len(ids) and a == 0 and q == 0:
+            break
+    assert len(done) == len(ids)
+    for jid, sc in zip(ids, scs):
+        parts, dens = done[jid]
+        ref = alone(sc)
+        assert parts.tobytes() == ref.tobytes(), sc.name
+        rho = ref["pressure"] / np.float32(sc.params.gas_constant) + np.float32(sc.params.rest_density)
+        assert np.array_equal(dens, rho.astype(np.float32))
+
+
+def test_budget_admission_and_rejection():
+    small = job(2000, 5, 7)
+    per_job = Server.job_bytes(small.n, small.s)
+    srv = Server(budget_bytes=int(per_job * 1.5), max_slots=8)
+    big = job(20000, 5, 8)
+    with pytest.raises(SphError) as ei:
+        srv.submit(big)
+    assert ei.value.status == 7
+    a_id = srv.submit(small)
+    b_id = srv.submit(job(2000, 5, 9))
+    a, q = srv.poll(2)
+    assert a == 1 and q == 1          # the second job waits for budget
+    for _ in range(20):
+        a, q = srv.poll(2)
+        if a == 0 and q == 0:
+            break
+    assert srv.result(a_id) is not None and srv.result(b_id) is not None
+
+
+def test_malformed_jobs_rejected():
+    srv = Server(budget_bytes=1 << 28, max_slots=2)
+    sc = job(100, 5, 1)
+    with pytest.raises(SphError) as ei:
+        srv.submit(sc, steps=0)
+    assert ei.value.status == 1
+    sc.params.h = -1.0
+    with pytest.raises(SphError):
+        srv.submit(sc)
+    with pytest.raises(SphError):
+        Server(budget_bytes=0)

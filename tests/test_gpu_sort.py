@@ -62,6 +62,20 @@ def test_sort_cell_boundaries_and_coincident():
     check_sort(pos, float(h), 2 * pos.shape[0])
 
 
+def test_sort_oversized_bucket_membership():
+    """A bucket above the stable-rank limit (8192 members) keeps arrival
+    order: membership and tables stay exact, the order inside it is not
+    promised."""
+    rng = np.random.default_rng(5)
+    pos = rng.uniform(0.1, 0.2, size=(10000, 3)).astype(np.float32)
+    keys, counts, starts, order = cell_sort(pos, 1.0, 3)
+    ref_keys = oracle_hash(pos, 1.0, 3)
+    assert np.array_equal(keys, ref_keys)
+    ref_counts, ref_starts, _ = oracle_counting_sort(ref_keys, 3)
+    assert np.array_equal(counts, ref_counts) and np.array_equal(starts, ref_starts)
+    assert np.array_equal(np.sort(order), np.arange(10000, dtype=np.uint32))
+
+
 def test_sort_single_and_tiny():
     check_sort(np.array([[0.5, 0.5, 0.5]], np.float32), 1.0, 2)
     check_sort(np.array([[0.5, 0.5, 0.5], [0.5, 0.5, 0.5]], np.float32), 1.0, 4)
