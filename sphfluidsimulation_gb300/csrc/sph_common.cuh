@@ -5,6 +5,7 @@
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <algorithm>
 
 #define SPH_HD __host__ __device__ __forceinline__
 
@@ -109,8 +110,10 @@ struct SceneDesc {
     uint32_t s_off, s;
     uint32_t sq_off, t;
     uint32_t t_off, pad0;
+    uint32_t sf_off, sf_buckets;   // neighbour-pass static table (power of two >= 8 s)
     FastMod fm_b;
     FastMod fm_s;
+    FastMod fm_sf;
     float h, h2;
     float mass, gas;
     float rho0, visc;
@@ -127,6 +130,19 @@ struct Tile {
     uint32_t end;
     uint32_t pad;
 };
+
+// Size of the static table the neighbour passes use: a power of two of at
+// least 8 s buckets, so aliasing between distant wall cells is rare.  The
+// reference's own s-bucket table (SimulationEngineCPU.cpp:468) is kept too,
+// for readback.
+inline uint32_t fast_static_buckets(uint32_t s)
+{
+    if (!s) return 0;
+    uint64_t want = std::max<uint64_t>(64, 8ull * s);
+    uint64_t b = 1;
+    while (b < want) b <<= 1;
+    return (uint32_t)std::min<uint64_t>(b, 1ull << 30);
+}
 
 // Smoothing kernel constant and self density (SF:115-125 as used by
 // SimulationEngineCPU.cpp:406-407), evaluated in float with the reference's

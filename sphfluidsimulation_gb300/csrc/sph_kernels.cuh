@@ -41,13 +41,18 @@ struct StepArgs {
     uint32_t scan_len;          // entries of count/start scanned
     unsigned long long* scan_status;
     uint32_t* scan_ticket;
-    const float4* spos;         // sorted static particles
-    const uint32_t* sstart;     // static bucket table (global scan)
+    const float4* spos;         // static particles sorted for the neighbour passes
+    const uint32_t* sstart;     // their bucket table (global scan, power-of-two buckets)
     const float* tris;          // 9 floats per triangle
     float4* accel;              // optional: acceleration per sorted slot (.w unused)
     uint32_t* err;              // device status word
     uint32_t* bar_count;        // grid barrier (persistent kernel only)
     uint32_t* bar_gen;
+    uint32_t* nbr;              // neighbour lists [k][stride]
+    uint32_t* snbr;
+    uint32_t* ncount;
+    uint32_t* tile_overflow;
+    uint32_t nbr_stride;
 };
 
 // ---- small helpers ---------------------------------------------------------
@@ -396,65 +401,220 @@ __device__ __forceinline__ float dist2(const float4& q, const float4& p)
 
 // ---- stage: density / pressure ---------------------------------------------
 //
-// UpdateParticlePressure (SF:358-501): for the 27 buckets of the cell
-// neighbourhood (bucket ids repeat if cells collide, as in the reference),
-// sum (h - r)^3 over dynamic neighbours (self skipped) and static neighbours
-// within h; rho = selfDensity + (sum_d m + sum_s m) C; p = k (rho - rho0).
-__device__ __forceinline__ void density_tile(const Tile& tile, const SceneDesc* scenes, const float4* __restrict__ pos,
+// UpdateParticlePressure (SF:358-501): over the 27 buckets of the cell
+// neighbourhood (x outermost, bucket ids repeating where cells collide, as in
+// the reference), sum (h - r)^3 over dynamic neighbours (self skipped) and
+// static neighbours within h; rho = selfDensity + (sum_d m + sum_s m) C and
+// p = k (rho - rho0), stored in vel.w.
+//
+// The pass runs in two loops.  The test loop visits every candidate and
+// appends the slot of each one with r^2 <= h^2 to the particle's neighbour
+// list (column layout nbr[k * stride + i]).  The sum loop then walks the list,
+// so the square root and the kernel polynomial run once per neighbour
+// instead of under divergence for every candidate.  The force pass reuses the
+// same list.  A particle with more than kMaxNbr dynamic or kMaxSNbr static
+// neighbours is flagged (kOverflow) and summed by re-walking its buckets.
+//
+// Neighbour cells whose box lies farther than h from the particle hold no
+// neighbour and are skipped, provided the 27 bucket ids are distinct (their
+// Morton codes span less than the bucket count); otherwise all 27 are walked.
+
+constexpr uint32_t kMaxNbr = 96;        // dynamic neighbours listed per particle
+constexpr uint32_t kMaxSNbr = 48;       // static neighbours listed per particle
+constexpr uint32_t kOverflow = 0xFFFFu;
+
+struct NbrArgs {
+    uint32_t* nbr;         // [kMaxNbr][stride]
+    uint32_t* snbr;        // [kMaxSNbr][stride]
+    uint32_t* ncount;      // dynamic count | static count << 16
+    uint32_t* tile_overflow;
+    uint32_t stride;
+};
+
+__device__ __forceinline__ float pick3f(int k, float v0, float v1, float v2)
+{
+    return k == 0 ? v0 : (k == 1 ? v1 : v2);
+}
+
+__device__ __forceinline__ uint32_t span3(uint32_t a, uint32_t b, uint32_t c)
+{
+    return max(max(a, b), c) - min(min(a, b), c);
+}
+
+// Squared distances from the particle to the boxes of its neighbour cells
+// along one axis: offset -1, 0, +1.  Conservative (cull threshold carries a
+// relative margin) and disabled far from the origin where the float cell
+// corner is inexact.
+struct CellBox {
+    float x0, x2, y0, y2, z0, z2;   // squared face distances (offset 0 -> 0)
+    bool ok;
+};
+
+__device__ __forceinline__ CellBox cell_box(const float4& p, float h)
+{
+    CellBox b;
+    const int32_t cx = (int32_t)cell_coord(p.x, h), cy = (int32_t)cell_coord(p.y, h), cz = (int32_t)cell_coord(p.z, h);
+    b.ok = abs(cx) < (1 << 22) && abs(cy) < (1 << 22) && abs(cz) < (1 << 22);
+    const float fx = p.x - (float)cx * h, fy = p.y - (float)cy * h, fz = p.z - (float)cz * h;
+    const float gx = fmaxf(h - fx, 0.f), gy = fmaxf(h - fy, 0.f), gz = fmaxf(h - fz, 0.f);
+    const float ax = fmaxf(fx, 0.f), ay = fmaxf(fy, 0.f), az = fmaxf(fz, 0.f);
+    b.x0 = ax * ax; b.x2 = gx * gx;
+    b.y0 = ay * ay; b.y2 = gy * gy;
+    b.z0 = az * az; b.z2 = gz * gz;
+    return b;
+}
+
+__device__ __forceinline__ uint32_t nb_span(const Neighbourhood& nb)
+{
+    return span3(nb.ex0, nb.ex1, nb.ex2) + span3(nb.ey0, nb.ey1, nb.ey2) + span3(nb.ez0, nb.ez1, nb.ez2);
+}
+
+// How many of the 27 neighbour cells share cell k's bucket in the reference's
+// s-bucket static table (hash % s): the reference walks that bucket once per
+// such cell, so each static neighbour in cell k counts that many times
+// (SF:452-490 with SimulationEngineCPU.cpp:468).  1 unless the neighbourhood's
+// Morton codes span at least s.
+__device__ __noinline__ inline uint32_t static_multiplicity(const Neighbourhood& nb, const FastMod& fm_s, uint32_t hk)
+{
+    const uint32_t target = fast_mod(hk, fm_s);
+    uint32_t m = 0;
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+            for (int c = 0; c < 3; ++c)
+                m += fast_mod(neighbour_hash(nb, a, b, c), fm_s) == target ? 1u : 0u;
+    return m;
+}
+
+constexpr uint32_t kMultShift = 27;                    // static list entry: index | multiplicity << 27
+constexpr uint32_t kIndexMask = (1u << kMultShift) - 1u;
+
+__device__ __forceinline__ float w0_of(float r2, float h)
+{
+    const float r = __fsqrt_rn(r2);
+    const float w = __fsub_rn(h, r);
+    return r < h ? __fmul_rn(__fmul_rn(w, w), w) : 0.f;
+}
+
+__device__ __forceinline__ void density_tile(uint32_t tile_index, const Tile& tile, const SceneDesc* scenes,
+                                             const float4* __restrict__ pos,
                                              float4* __restrict__ vel, const uint32_t* __restrict__ start,
-                                             const float4* __restrict__ spos, const uint32_t* __restrict__ sstart)
+                                             const float4* __restrict__ spos, const uint32_t* __restrict__ sstart,
+                                             const NbrArgs& nl)
 {
     const SceneDesc& sc = scenes[tile.scene];
     const uint32_t i = tile.begin + threadIdx.x;
-    if (i >= tile.end) return;
-    const float h = sc.h, h2 = sc.h2;
-    const float4 p = pos[i];
-    const Neighbourhood nb = neighbourhood(p.x, p.y, p.z, h);
-    const uint32_t delta = sc.p_off - __ldg(start + sc.q_off);
-    const uint32_t sdelta = sc.s ? sc.s_off - __ldg(sstart + sc.sq_off) : 0u;
-    float sum_d = 0.f, sum_s = 0.f;
+    bool overflow = false;
+    if (i < tile.end) {
+        const float h = sc.h, h2 = sc.h2;
+        const float cull2 = __fmul_rn(h2, 1.0001f);
+        const float4 p = pos[i];
+        const Neighbourhood nb = neighbourhood(p.x, p.y, p.z, h);
+        const CellBox box = cell_box(p, h);
+        const uint32_t span = nb_span(nb);
+        const bool cull_d = box.ok && span < sc.buckets;
+        const bool dup_s = span >= sc.s;     // reference static buckets may repeat
+        const uint32_t delta = sc.p_off - __ldg(start + sc.q_off);
+        const uint32_t sdelta = sc.s ? sc.s_off - __ldg(sstart + sc.sf_off) : 0u;
+        const uint32_t stride = nl.stride;
+        uint32_t cnt = 0, scnt = 0;
 #pragma unroll 1
-    for (int a = 0; a < 3; ++a)
+        for (int a = 0; a < 3; ++a)
 #pragma unroll 1
-        for (int b = 0; b < 3; ++b)
+            for (int b = 0; b < 3; ++b)
 #pragma unroll 1
-            for (int c = 0; c < 3; ++c) {
-                const uint32_t hsh = neighbour_hash(nb, a, b, c);
-                const uint32_t bk = sc.q_off + fast_mod(hsh, sc.fm_b);
-                const uint32_t beg = max(__ldg(start + bk) + delta, sc.p_off);
-                const uint32_t end = min(__ldg(start + bk + 1) + delta, sc.p_off + sc.n);
-                for (uint32_t j = beg; j < end; ++j) {
-                    const float4 q = __ldg(pos + j);
-                    const float r2 = dist2(q, p);
-                    if (r2 <= h2 && j != i) {
-                        const float r = __fsqrt_rn(r2);
-                        if (r < h) {
-                            const float w = __fsub_rn(h, r);
-                            sum_d = __fmaf_rn(__fmul_rn(w, w), w, sum_d);
+                for (int c = 0; c < 3; ++c) {
+                    const float bd2 = pick3f(a, box.x0, 0.f, box.x2) + pick3f(b, box.y0, 0.f, box.y2) +
+                                      pick3f(c, box.z0, 0.f, box.z2);
+                    const bool far = bd2 > cull2;
+                    const uint32_t hsh = neighbour_hash(nb, a, b, c);
+                    if (!(far && cull_d)) {
+                        const uint32_t bk = sc.q_off + fast_mod(hsh, sc.fm_b);
+                        const uint32_t beg = max(__ldg(start + bk) + delta, sc.p_off);
+                        const uint32_t end = min(__ldg(start + bk + 1) + delta, sc.p_off + sc.n);
+                        for (uint32_t j = beg; j < end; ++j) {
+                            const float4 q = __ldg(pos + j);
+                            if (dist2(q, p) <= h2 && j != i) {
+                                if (cnt < kMaxNbr) nl.nbr[(size_t)cnt * stride + i] = j;
+                                ++cnt;
+                            }
                         }
                     }
-                }
-                if (sc.s) {
-                    const uint32_t sb = sc.sq_off + fast_mod(hsh, sc.fm_s);
-                    const uint32_t sbeg = max(__ldg(sstart + sb) + sdelta, sc.s_off);
-                    const uint32_t send = min(__ldg(sstart + sb + 1) + sdelta, sc.s_off + sc.s);
-                    for (uint32_t j = sbeg; j < send; ++j) {
-                        const float4 q = __ldg(spos + j);
-                        const float r2 = dist2(q, p);
-                        if (r2 <= h2) {
-                            const float r = __fsqrt_rn(r2);
-                            if (r < h) {
-                                const float w = __fsub_rn(h, r);
-                                sum_s = __fmaf_rn(__fmul_rn(w, w), w, sum_s);
+                    if (sc.s && !(far && box.ok)) {
+                        const uint32_t sb = sc.sf_off + fast_mod(hsh, sc.fm_sf);
+                        const uint32_t sbeg = max(__ldg(sstart + sb) + sdelta, sc.s_off);
+                        const uint32_t send = min(__ldg(sstart + sb + 1) + sdelta, sc.s_off + sc.s);
+                        uint32_t mult = 0;
+                        for (uint32_t j = sbeg; j < send; ++j) {
+                            const float4 q = __ldg(spos + j);
+                            // statics carry their cell's Morton code: only this cell's count
+                            if (__float_as_uint(q.w) == hsh && dist2(q, p) <= h2) {
+                                if (!mult) mult = dup_s ? static_multiplicity(nb, sc.fm_s, hsh) : 1u;
+                                if (scnt < kMaxSNbr) nl.snbr[(size_t)scnt * stride + i] = j | (mult << kMultShift);
+                                ++scnt;
                             }
                         }
                     }
                 }
+        float sum_d = 0.f, sum_s = 0.f;
+        if (cnt <= kMaxNbr) {
+            const uint32_t* lp = nl.nbr + i;
+            for (uint32_t k = 0; k < cnt; ++k, lp += stride) {
+                const uint32_t j = *lp;
+                sum_d = __fadd_rn(sum_d, w0_of(dist2(__ldg(pos + j), p), h));
             }
-    const float rho = __fadd_rn(sc.self_density,
-                                __fmul_rn(__fadd_rn(__fmul_rn(sum_d, sc.mass), __fmul_rn(sum_s, sc.mass)), sc.kc));
-    const float pressure = __fmul_rn(sc.gas, __fsub_rn(rho, sc.rho0));
-    reinterpret_cast<float*>(vel + i)[3] = pressure;
+        }
+        if (scnt <= kMaxSNbr) {
+            const uint32_t* lp = nl.snbr + i;
+            for (uint32_t k = 0; k < scnt; ++k, lp += stride) {
+                const uint32_t e = *lp;
+                const float w0 = w0_of(dist2(__ldg(spos + (e & kIndexMask)), p), h);
+                for (uint32_t m = e >> kMultShift; m; --m) sum_s = __fadd_rn(sum_s, w0);
+            }
+        }
+        if (cnt > kMaxNbr || scnt > kMaxSNbr) {
+            // overflow: walk the buckets again, summing directly
+#pragma unroll 1
+            for (int a = 0; a < 3; ++a)
+#pragma unroll 1
+                for (int b = 0; b < 3; ++b)
+#pragma unroll 1
+                    for (int c = 0; c < 3; ++c) {
+                        const uint32_t hsh = neighbour_hash(nb, a, b, c);
+                        if (cnt > kMaxNbr) {
+                            const uint32_t bk = sc.q_off + fast_mod(hsh, sc.fm_b);
+                            const uint32_t beg = max(__ldg(start + bk) + delta, sc.p_off);
+                            const uint32_t end = min(__ldg(start + bk + 1) + delta, sc.p_off + sc.n);
+                            for (uint32_t j = beg; j < end; ++j) {
+                                const float r2 = dist2(__ldg(pos + j), p);
+                                if (r2 <= h2 && j != i) sum_d = __fadd_rn(sum_d, w0_of(r2, h));
+                            }
+                        }
+                        if (sc.s && scnt > kMaxSNbr) {
+                            const uint32_t sb = sc.sf_off + fast_mod(hsh, sc.fm_sf);
+                            const uint32_t sbeg = max(__ldg(sstart + sb) + sdelta, sc.s_off);
+                            const uint32_t send = min(__ldg(sstart + sb + 1) + sdelta, sc.s_off + sc.s);
+                            uint32_t mult = 0;
+                            for (uint32_t j = sbeg; j < send; ++j) {
+                                const float4 q = __ldg(spos + j);
+                                const float r2 = dist2(q, p);
+                                if (__float_as_uint(q.w) == hsh && r2 <= h2) {
+                                    if (!mult) mult = dup_s ? static_multiplicity(nb, sc.fm_s, hsh) : 1u;
+                                    const float w0 = w0_of(r2, h);
+                                    for (uint32_t m = mult; m; --m) sum_s = __fadd_rn(sum_s, w0);
+                                }
+                            }
+                        }
+                    }
+            overflow = true;
+        }
+        nl.ncount[i] = (cnt > kMaxNbr ? kOverflow : cnt) | ((scnt > kMaxSNbr ? kOverflow : scnt) << 16);
+        const float rho = __fadd_rn(sc.self_density,
+                                    __fmul_rn(__fadd_rn(__fmul_rn(sum_d, sc.mass), __fmul_rn(sum_s, sc.mass)), sc.kc));
+        const float pressure = __fmul_rn(sc.gas, __fsub_rn(rho, sc.rho0));
+        reinterpret_cast<float*>(vel + i)[3] = pressure;
+    }
+    const int any = __syncthreads_or(overflow ? 1 : 0);
+    if (threadIdx.x == 0) nl.tile_overflow[tile_index] = any ? 1u : 0u;
 }
 
 // ---- stage: force + integrate + rehash -------------------------------------
@@ -464,31 +624,175 @@ __device__ __forceinline__ void density_tile(const Tile& tile, const SceneDesc* 
 // neighbours (their viscosity term is multiplied by 0 in the reference,
 // SF:629, and is omitted); scale by m / (2 rho_i) C and mu m C; add triangle
 // forces; a = F / rho_i + g; semi-implicit Euler; new key; count.
+//
+// The neighbours come from the density pass's list, in the same order as the
+// buckets were walked.  Particles whose list overflowed are left to
+// force_overflow_tile, which walks their buckets.
+
+struct PairSums {
+    float3 fp, fv, fs;
+};
+
+__device__ __forceinline__ void add_dynamic_pair(PairSums& s, const float4& p, const float4& v, float pi, float h,
+                                                 const float4& q, const float4& u)
+{
+    float dx = __fsub_rn(q.x, p.x), dy = __fsub_rn(q.y, p.y), dz = __fsub_rn(q.z, p.z);
+    const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+    const float r = __fsqrt_rn(r2);
+    if (!(r < h)) return;
+    if (r2 == 0.f || r == 0.f) {
+        const float3 d = random_direction((float)__float_as_uint(p.w));
+        dx = d.x; dy = d.y; dz = d.z;
+    } else {
+        const float inv = __frcp_rn(r);
+        dx = __fmul_rn(dx, inv); dy = __fmul_rn(dy, inv); dz = __fmul_rn(dz, inv);
+    }
+    const float w = __fsub_rn(h, r);
+    const float w1 = __fmul_rn(__fmul_rn(-3.f, w), w);
+    const float w2 = __fmul_rn(6.f, w);
+    const float pp = __fmul_rn(__fadd_rn(pi, u.w), w1);
+    s.fp.x = __fmaf_rn(dx, pp, s.fp.x);
+    s.fp.y = __fmaf_rn(dy, pp, s.fp.y);
+    s.fp.z = __fmaf_rn(dz, pp, s.fp.z);
+    s.fv.x = __fmaf_rn(__fsub_rn(u.x, v.x), w2, s.fv.x);
+    s.fv.y = __fmaf_rn(__fsub_rn(u.y, v.y), w2, s.fv.y);
+    s.fv.z = __fmaf_rn(__fsub_rn(u.z, v.z), w2, s.fv.z);
+}
+
+__device__ __forceinline__ void add_static_pair(PairSums& s, const float4& p, float api, float h, const float4& q)
+{
+    float dx = __fsub_rn(q.x, p.x), dy = __fsub_rn(q.y, p.y), dz = __fsub_rn(q.z, p.z);
+    const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+    const float r = __fsqrt_rn(r2);
+    if (!(r < h)) return;
+    if (r2 == 0.f || r == 0.f) {
+        const float3 d = random_direction((float)__float_as_uint(p.w));
+        dx = d.x; dy = d.y; dz = d.z;
+    } else {
+        const float inv = __frcp_rn(r);
+        dx = __fmul_rn(dx, inv); dy = __fmul_rn(dy, inv); dz = __fmul_rn(dz, inv);
+    }
+    const float w = __fsub_rn(h, r);
+    const float pp = __fmul_rn(api, __fmul_rn(__fmul_rn(-3.f, w), w));
+    s.fs.x = __fmaf_rn(dx, pp, s.fs.x);
+    s.fs.y = __fmaf_rn(dy, pp, s.fs.y);
+    s.fs.z = __fmaf_rn(dz, pp, s.fs.z);
+}
+
+// SF:626-645: scale the sums, add triangle forces and gravity, integrate,
+// store the moved particle and its new key.
+template <bool kRecordAccel>
+__device__ __forceinline__ uint32_t integrate_particle(const SceneDesc& sc, uint32_t i, const float4& p, const float4& v,
+                                                       float rho, const PairSums& s, const float* __restrict__ tris,
+                                                       float4* __restrict__ pos_out, float4* __restrict__ vel_out,
+                                                       uint32_t* __restrict__ key_out, float4* accel)
+{
+    const float s1 = __fmul_rn(__fdiv_rn(sc.mass, __fmul_rn(2.f, rho)), sc.kc);
+    const float s2 = __fmul_rn(__fmul_rn(sc.visc, sc.mass), sc.kc);
+    float3 f;
+    f.x = __fadd_rn(__fadd_rn(__fmul_rn(s.fp.x, s1), __fmul_rn(s.fv.x, s2)), __fmul_rn(s.fs.x, s1));
+    f.y = __fadd_rn(__fadd_rn(__fmul_rn(s.fp.y, s1), __fmul_rn(s.fv.y, s2)), __fmul_rn(s.fs.y, s1));
+    f.z = __fadd_rn(__fadd_rn(__fmul_rn(s.fp.z, s1), __fmul_rn(s.fv.z, s2)), __fmul_rn(s.fs.z, s1));
+    for (uint32_t t = 0; t < sc.t; ++t) {
+        const float3 tf = triangle_force(make_float3(p.x, p.y, p.z), tris + 9u * (sc.t_off + t));
+        f.x = __fadd_rn(f.x, tf.x); f.y = __fadd_rn(f.y, tf.y); f.z = __fadd_rn(f.z, tf.z);
+    }
+    float3 acc;
+    acc.x = __fadd_rn(__fdiv_rn(f.x, rho), sc.gx);
+    acc.y = __fadd_rn(__fdiv_rn(f.y, rho), sc.gy);
+    acc.z = __fadd_rn(__fdiv_rn(f.z, rho), sc.gz);
+    float3 nv, np;
+    nv.x = __fadd_rn(v.x, __fmul_rn(acc.x, sc.dt));
+    nv.y = __fadd_rn(v.y, __fmul_rn(acc.y, sc.dt));
+    nv.z = __fadd_rn(v.z, __fmul_rn(acc.z, sc.dt));
+    np.x = __fadd_rn(p.x, __fmul_rn(nv.x, sc.dt));
+    np.y = __fadd_rn(p.y, __fmul_rn(nv.y, sc.dt));
+    np.z = __fadd_rn(p.z, __fmul_rn(nv.z, sc.dt));
+    const uint32_t k = fast_mod(cell_hash(np.x, np.y, np.z, sc.h), sc.fm_b);
+    pos_out[i] = make_float4(np.x, np.y, np.z, p.w);
+    vel_out[i] = make_float4(nv.x, nv.y, nv.z, v.w);
+    key_out[i] = k;
+    if (kRecordAccel) accel[i] = make_float4(acc.x, acc.y, acc.z, 0.f);
+    return k;
+}
+
 template <bool kRecordAccel>
 __device__ __forceinline__ void force_tile(const Tile& tile, const SceneDesc* scenes, const float4* __restrict__ pos,
-                                           const float4* __restrict__ vel, const uint32_t* __restrict__ start,
-                                           const float4* __restrict__ spos, const uint32_t* __restrict__ sstart,
-                                           const float* __restrict__ tris, float4* __restrict__ pos_out,
-                                           float4* __restrict__ vel_out, uint32_t* __restrict__ key_out,
-                                           uint32_t* __restrict__ arrival, uint32_t* count, float4* accel)
+                                           const float4* __restrict__ vel, const float4* __restrict__ spos,
+                                           const float* __restrict__ tris, const NbrArgs& nl,
+                                           float4* __restrict__ pos_out, float4* __restrict__ vel_out,
+                                           uint32_t* __restrict__ key_out, uint32_t* __restrict__ arrival,
+                                           uint32_t* count, float4* accel)
 {
     const SceneDesc& sc = scenes[tile.scene];
     const uint32_t i = tile.begin + threadIdx.x;
-    const bool valid = i < tile.end;
-    uint32_t g = 0, k = 0;
+    bool valid = i < tile.end;
+    uint32_t g = 0;
+    if (valid) {
+        const uint32_t c = nl.ncount[i];
+        const uint32_t cd = c & 0xFFFFu, cs = c >> 16;
+        if (cd == kOverflow || cs == kOverflow) {
+            valid = false;                         // handled by force_overflow_tile
+        } else {
+            const float h = sc.h;
+            const float4 p = pos[i];
+            const float4 v = vel[i];
+            const float pi = v.w;
+            const float rho = __fadd_rn(__fdiv_rn(pi, sc.gas), sc.rho0);
+            const uint32_t stride = nl.stride;
+            PairSums s;
+            s.fp = s.fv = s.fs = make_float3(0.f, 0.f, 0.f);
+            const uint32_t* lp = nl.nbr + i;
+#pragma unroll 2
+            for (uint32_t k = 0; k < cd; ++k, lp += stride) {
+                const uint32_t j = __ldg(lp);
+                add_dynamic_pair(s, p, v, pi, h, __ldg(pos + j), __ldg(vel + j));
+            }
+            const float api = fabsf(pi);
+            lp = nl.snbr + i;
+            for (uint32_t k = 0; k < cs; ++k, lp += stride) {
+                const uint32_t e = __ldg(lp);
+                const float4 q = __ldg(spos + (e & kIndexMask));
+                for (uint32_t m = e >> kMultShift; m; --m) add_static_pair(s, p, api, h, q);
+            }
+            g = sc.q_off + integrate_particle<kRecordAccel>(sc, i, p, v, rho, s, tris, pos_out, vel_out, key_out, accel);
+        }
+    }
+    const uint32_t r = warp_aggregated_increment(count, g, valid);
+    if (valid) arrival[i] = r;
+}
+
+// Overflow particles: the same sums, walking the 27 buckets directly.
+template <bool kRecordAccel>
+__device__ __forceinline__ void force_overflow_tile(const Tile& tile, const SceneDesc* scenes, const float4* __restrict__ pos,
+                                                    const float4* __restrict__ vel, const uint32_t* __restrict__ start,
+                                                    const float4* __restrict__ spos, const uint32_t* __restrict__ sstart,
+                                                    const float* __restrict__ tris, const NbrArgs& nl,
+                                                    float4* __restrict__ pos_out, float4* __restrict__ vel_out,
+                                                    uint32_t* __restrict__ key_out, uint32_t* __restrict__ arrival,
+                                                    uint32_t* count, float4* accel)
+{
+    const SceneDesc& sc = scenes[tile.scene];
+    const uint32_t i = tile.begin + threadIdx.x;
+    bool valid = false;
+    uint32_t g = 0;
+    if (i < tile.end) {
+        const uint32_t c = nl.ncount[i];
+        valid = (c & 0xFFFFu) == kOverflow || (c >> 16) == kOverflow;
+    }
     if (valid) {
         const float h = sc.h, h2 = sc.h2;
         const float4 p = pos[i];
         const float4 v = vel[i];
         const float pi = v.w;
+        const float api = fabsf(pi);
         const float rho = __fadd_rn(__fdiv_rn(pi, sc.gas), sc.rho0);
         const Neighbourhood nb = neighbourhood(p.x, p.y, p.z, h);
         const uint32_t delta = sc.p_off - __ldg(start + sc.q_off);
-        const uint32_t sdelta = sc.s ? sc.s_off - __ldg(sstart + sc.sq_off) : 0u;
-        float3 fp = make_float3(0.f, 0.f, 0.f);   // dynamic pressure
-        float3 fv = make_float3(0.f, 0.f, 0.f);   // dynamic viscosity
-        float3 fs = make_float3(0.f, 0.f, 0.f);   // static pressure
-        const float api = fabsf(pi);
+        const uint32_t sdelta = sc.s ? sc.s_off - __ldg(sstart + sc.sf_off) : 0u;
+        const bool span_s_dup = nb_span(nb) >= sc.s;
+        PairSums s;
+        s.fp = s.fv = s.fs = make_float3(0.f, 0.f, 0.f);
 #pragma unroll 1
         for (int a = 0; a < 3; ++a)
 #pragma unroll 1
@@ -501,88 +805,23 @@ __device__ __forceinline__ void force_tile(const Tile& tile, const SceneDesc* sc
                     const uint32_t end = min(__ldg(start + bk + 1) + delta, sc.p_off + sc.n);
                     for (uint32_t j = beg; j < end; ++j) {
                         const float4 q = __ldg(pos + j);
-                        float dx = __fsub_rn(q.x, p.x), dy = __fsub_rn(q.y, p.y), dz = __fsub_rn(q.z, p.z);
-                        const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-                        if (r2 <= h2 && j != i) {
-                            const float r = __fsqrt_rn(r2);
-                            if (r < h) {
-                                const float4 u = __ldg(vel + j);
-                                if (r2 == 0.f || r == 0.f) {
-                                    const float3 d = random_direction((float)__float_as_uint(p.w));
-                                    dx = d.x; dy = d.y; dz = d.z;
-                                } else {
-                                    const float inv = __frcp_rn(r);
-                                    dx = __fmul_rn(dx, inv); dy = __fmul_rn(dy, inv); dz = __fmul_rn(dz, inv);
-                                }
-                                const float w = __fsub_rn(h, r);
-                                const float w1 = __fmul_rn(__fmul_rn(-3.f, w), w);
-                                const float w2 = __fmul_rn(6.f, w);
-                                const float pp = __fmul_rn(__fadd_rn(pi, u.w), w1);
-                                fp.x = __fmaf_rn(dx, pp, fp.x);
-                                fp.y = __fmaf_rn(dy, pp, fp.y);
-                                fp.z = __fmaf_rn(dz, pp, fp.z);
-                                fv.x = __fmaf_rn(__fsub_rn(u.x, v.x), w2, fv.x);
-                                fv.y = __fmaf_rn(__fsub_rn(u.y, v.y), w2, fv.y);
-                                fv.z = __fmaf_rn(__fsub_rn(u.z, v.z), w2, fv.z);
-                            }
-                        }
+                        if (dist2(q, p) <= h2 && j != i) add_dynamic_pair(s, p, v, pi, h, q, __ldg(vel + j));
                     }
                     if (sc.s) {
-                        const uint32_t sb = sc.sq_off + fast_mod(hsh, sc.fm_s);
+                        const uint32_t sb = sc.sf_off + fast_mod(hsh, sc.fm_sf);
                         const uint32_t sbeg = max(__ldg(sstart + sb) + sdelta, sc.s_off);
                         const uint32_t send = min(__ldg(sstart + sb + 1) + sdelta, sc.s_off + sc.s);
+                        uint32_t mult = 0;
                         for (uint32_t j = sbeg; j < send; ++j) {
                             const float4 q = __ldg(spos + j);
-                            float dx = __fsub_rn(q.x, p.x), dy = __fsub_rn(q.y, p.y), dz = __fsub_rn(q.z, p.z);
-                            const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-                            if (r2 <= h2) {
-                                const float r = __fsqrt_rn(r2);
-                                if (r < h) {
-                                    if (r2 == 0.f || r == 0.f) {
-                                        const float3 d = random_direction((float)__float_as_uint(p.w));
-                                        dx = d.x; dy = d.y; dz = d.z;
-                                    } else {
-                                        const float inv = __frcp_rn(r);
-                                        dx = __fmul_rn(dx, inv); dy = __fmul_rn(dy, inv); dz = __fmul_rn(dz, inv);
-                                    }
-                                    const float w = __fsub_rn(h, r);
-                                    const float pp = __fmul_rn(api, __fmul_rn(__fmul_rn(-3.f, w), w));
-                                    fs.x = __fmaf_rn(dx, pp, fs.x);
-                                    fs.y = __fmaf_rn(dy, pp, fs.y);
-                                    fs.z = __fmaf_rn(dz, pp, fs.z);
-                                }
+                            if (__float_as_uint(q.w) == hsh && dist2(q, p) <= h2) {
+                                if (!mult) mult = span_s_dup ? static_multiplicity(nb, sc.fm_s, hsh) : 1u;
+                                for (uint32_t m = mult; m; --m) add_static_pair(s, p, api, h, q);
                             }
                         }
                     }
                 }
-        // SF:626-642 in the reference's operation order, without contraction
-        const float s1 = __fmul_rn(__fdiv_rn(sc.mass, __fmul_rn(2.f, rho)), sc.kc);
-        const float s2 = __fmul_rn(__fmul_rn(sc.visc, sc.mass), sc.kc);
-        float3 f;
-        f.x = __fadd_rn(__fadd_rn(__fmul_rn(fp.x, s1), __fmul_rn(fv.x, s2)), __fmul_rn(fs.x, s1));
-        f.y = __fadd_rn(__fadd_rn(__fmul_rn(fp.y, s1), __fmul_rn(fv.y, s2)), __fmul_rn(fs.y, s1));
-        f.z = __fadd_rn(__fadd_rn(__fmul_rn(fp.z, s1), __fmul_rn(fv.z, s2)), __fmul_rn(fs.z, s1));
-        for (uint32_t t = 0; t < sc.t; ++t) {
-            const float3 tf = triangle_force(make_float3(p.x, p.y, p.z), tris + 9u * (sc.t_off + t));
-            f.x = __fadd_rn(f.x, tf.x); f.y = __fadd_rn(f.y, tf.y); f.z = __fadd_rn(f.z, tf.z);
-        }
-        float3 acc;
-        acc.x = __fadd_rn(__fdiv_rn(f.x, rho), sc.gx);
-        acc.y = __fadd_rn(__fdiv_rn(f.y, rho), sc.gy);
-        acc.z = __fadd_rn(__fdiv_rn(f.z, rho), sc.gz);
-        float3 nv, np;
-        nv.x = __fadd_rn(v.x, __fmul_rn(acc.x, sc.dt));
-        nv.y = __fadd_rn(v.y, __fmul_rn(acc.y, sc.dt));
-        nv.z = __fadd_rn(v.z, __fmul_rn(acc.z, sc.dt));
-        np.x = __fadd_rn(p.x, __fmul_rn(nv.x, sc.dt));
-        np.y = __fadd_rn(p.y, __fmul_rn(nv.y, sc.dt));
-        np.z = __fadd_rn(p.z, __fmul_rn(nv.z, sc.dt));
-        k = fast_mod(cell_hash(np.x, np.y, np.z, h), sc.fm_b);
-        g = sc.q_off + k;
-        pos_out[i] = make_float4(np.x, np.y, np.z, p.w);
-        vel_out[i] = make_float4(nv.x, nv.y, nv.z, pi);
-        key_out[i] = k;
-        if (kRecordAccel) accel[i] = make_float4(acc.x, acc.y, acc.z, 0.f);
+        g = sc.q_off + integrate_particle<kRecordAccel>(sc, i, p, v, rho, s, tris, pos_out, vel_out, key_out, accel);
     }
     const uint32_t r = warp_aggregated_increment(count, g, valid);
     if (valid) arrival[i] = r;

@@ -114,7 +114,7 @@ struct Job {
     std::vector<float> pos, spos;
     uint32_t steps = 0, done = 0;
     JobState state = JobState::Queued;
-    uint64_t p_off = 0, q_off = 0, s_off = 0, sq_off = 0;
+    uint64_t p_off = 0, q_off = 0, s_off = 0, sq_off = 0, sf_off = 0;
     uint64_t bytes = 0;
     std::vector<sph_dynamic_particle> result;
     float gas = 1.f, rho0 = 0.f;
@@ -131,9 +131,11 @@ double now_s()
 uint64_t job_bytes(uint32_t n, uint32_t s)
 {
     // per dynamic particle: sorted pos/vel 32, unsorted pos/vel 32, staging 32,
-    // key/arrival/perm 12, two buckets x (count + start) 16;
-    // per static particle: sorted 16, staging 32, bucket count + start 8
-    return 124ull * n + 56ull * s + 4096ull;
+    // key/arrival/perm 12, two buckets x (count + start) 16, neighbour lists
+    // (96 + 48 slots) 576, list counts 4;
+    // per static particle: two sorted copies 32, staging 32, bucket count +
+    // start for both tables 8 + 8 x 8 = 72
+    return 704ull * n + 136ull * s + 4096ull;
 }
 
 struct sph_server {
@@ -143,7 +145,7 @@ struct sph_server {
     uint32_t max_slots = 0;
     StepState arena;
     bool arena_ready = false;
-    RangeAlloc pa, qa, sa, sqa;
+    RangeAlloc pa, qa, sa, sqa, sfa;
     uint64_t used_bytes = 0;
     uint64_t next_id = 1;
     std::unordered_map<uint64_t, std::unique_ptr<Job>> jobs;
@@ -171,29 +173,33 @@ struct sph_server {
 static sph_status ensure_room(sph_server* sv, const Job& j)
 {
     const uint64_t n = j.in.n, s = j.in.s, q = 2ull * j.in.n + 1, sq = (uint64_t)j.in.s + 1;
+    const uint64_t sf = (uint64_t)sph::fast_static_buckets(j.in.s) + 1;
     uint64_t need_n = sv->pa.needed_for(n), need_q = sv->qa.needed_for(q);
-    uint64_t need_s = sv->sa.needed_for(s), need_sq = sv->sqa.needed_for(sq);
-    if (need_n <= sv->pa.cap() && need_q <= sv->qa.cap() && need_s <= sv->sa.cap() && need_sq <= sv->sqa.cap())
+    uint64_t need_s = sv->sa.needed_for(s), need_sq = sv->sqa.needed_for(sq), need_sf = sv->sfa.needed_for(sf);
+    if (need_n <= sv->pa.cap() && need_q <= sv->qa.cap() && need_s <= sv->sa.cap() && need_sq <= sv->sqa.cap() &&
+        need_sf <= sv->sfa.cap())
         return SPH_OK;
     auto grown = [](uint64_t need, uint64_t cap) { return need <= cap ? cap : std::max(need, cap * 2); };
     uint64_t cn = grown(need_n, sv->pa.cap()), cq = grown(need_q, sv->qa.cap());
     uint64_t cs = grown(need_s, sv->sa.cap()), csq = grown(need_sq, sv->sqa.cap());
+    uint64_t csf = grown(need_sf, sv->sfa.cap());
     const uint64_t limit = (1ull << 31) - 64;
-    if (cn > limit || cq > limit || cs > limit || csq > limit) {
+    if (cn > limit || cq > limit || cs > limit || csq > limit || csf > limit) {
         sph::set_last_error("arena index space exhausted");
         return SPH_ERR_CAPACITY;
     }
     if (!sv->arena_ready) {
         SRV_TRY(sv->arena.init_arena(sv->device, sv->stream, (uint32_t)cn, (uint32_t)cq, (uint32_t)cs, (uint32_t)csq,
-                                     sv->max_slots));
+                                     (uint32_t)csf, sv->max_slots));
         sv->arena_ready = true;
     } else {
-        SRV_TRY(sv->arena.grow_arena((uint32_t)cn, (uint32_t)cq, (uint32_t)cs, (uint32_t)csq));
+        SRV_TRY(sv->arena.grow_arena((uint32_t)cn, (uint32_t)cq, (uint32_t)cs, (uint32_t)csq, (uint32_t)csf));
     }
     sv->pa.grow(cn);
     sv->qa.grow(cq);
     sv->sa.grow(cs);
     sv->sqa.grow(csq);
+    sv->sfa.grow(csf);
     return SPH_OK;
 }
 
@@ -204,6 +210,7 @@ static SceneDesc desc_of(const Job& j)
     d.q_off = (uint32_t)j.q_off;
     d.s_off = (uint32_t)j.s_off;
     d.sq_off = (uint32_t)j.sq_off;
+    d.sf_off = (uint32_t)j.sf_off;
     return d;
 }
 
@@ -211,10 +218,12 @@ static sph_status admit(sph_server* sv, Job& j)
 {
     SRV_TRY(ensure_room(sv, j));
     const uint64_t n = j.in.n, q = 2ull * j.in.n + 1, s = j.in.s, sq = (uint64_t)j.in.s + 1;
+    const uint64_t sf = (uint64_t)sph::fast_static_buckets(j.in.s) + 1;
     bool ok = sv->pa.alloc(n, &j.p_off);
     ok = ok && sv->qa.alloc(q, &j.q_off);
     ok = ok && sv->sa.alloc(s, &j.s_off);
     ok = ok && sv->sqa.alloc(sq, &j.sq_off);
+    ok = ok && sv->sfa.alloc(sf, &j.sf_off);
     if (!ok) {
         sph::set_last_error("arena allocation failed after growth");
         return SPH_ERR_CAPACITY;
@@ -240,6 +249,7 @@ static void release_ranges(sph_server* sv, Job& j)
     sv->qa.release(j.q_off, 2ull * j.in.n + 1);
     sv->sa.release(j.s_off, j.in.s);
     sv->sqa.release(j.sq_off, (uint64_t)j.in.s + 1);
+    sv->sfa.release(j.sf_off, (uint64_t)sph::fast_static_buckets(j.in.s) + 1);
     sv->used_bytes -= j.bytes;
 }
 

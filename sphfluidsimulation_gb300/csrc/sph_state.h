@@ -79,9 +79,9 @@ public:
     // ---- arena mode (server): fixed-capacity arrays, each scene occupies
     // ranges of the slot / bucket / static index spaces chosen by the caller.
     sph_status init_arena(int device, cudaStream_t stream, uint32_t cap_n, uint32_t cap_q, uint32_t cap_s,
-                          uint32_t cap_sq, uint32_t max_scenes);
+                          uint32_t cap_sq, uint32_t cap_sf, uint32_t max_scenes);
     // Grows every array to at least the given capacities, keeping contents.
-    sph_status grow_arena(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s, uint32_t cap_sq);
+    sph_status grow_arena(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s, uint32_t cap_sq, uint32_t cap_sf);
     // Uploads one scene into its ranges (d's offsets) and sorts it alone.
     sph_status admit_scene(const SceneDesc& d, const SceneInput& in);
     // Replaces the set of scenes the step advances (table, tiles, scan range).
@@ -90,6 +90,7 @@ public:
     uint32_t cap_q() const { return cap_q_; }
     uint32_t cap_s() const { return cap_s_; }
     uint32_t cap_sq() const { return cap_sq_; }
+    uint32_t cap_sf() const { return cap_sf_; }
 
     const float* stage_ms() const { return stage_ms_; }
     void set_persistent_ctas(uint32_t c) { persistent_ctas_ = c; }
@@ -97,7 +98,7 @@ public:
     std::vector<SceneDesc> scenes;
     std::vector<Tile> tiles, stiles;
     uint32_t total_n = 0, total_s = 0, total_t = 0;
-    uint32_t scan_len = 0, sscan_len = 0;
+    uint32_t scan_len = 0, sscan_len = 0, sfscan_len = 0;
 
     // device arrays
     SceneDesc* d_scenes = nullptr;
@@ -110,23 +111,32 @@ public:
     uint32_t* scan_ticket = nullptr;
     uint32_t* err = nullptr;
     uint32_t* bar = nullptr;
-    float4* spos = nullptr;
+    float4* spos = nullptr;        // statics sorted by the neighbour-pass table
     uint32_t* sstart = nullptr;
+    float4* spos_ref = nullptr;    // statics sorted by the reference's s-bucket table
+    uint32_t* sstart_ref = nullptr;
+    uint32_t* nbr = nullptr;       // neighbour lists, [kMaxNbr][cap_n]
+    uint32_t* snbr = nullptr;      // [kMaxSNbr][cap_n]
+    uint32_t* ncount = nullptr;
+    uint32_t* tile_overflow = nullptr;
+    SceneDesc* d_sfscenes = nullptr;
     float* tris = nullptr;
     float4* accel = nullptr;
     float4* accel_io = nullptr;
     float4* staging = nullptr;
 
 private:
+    // sort kinds: 0 dynamic, 1 statics by the reference's table, 2 statics by
+    // the neighbour-pass table
     sph_status enqueue_load(const float4* src, bool statics);
-    sph_status enqueue_sort(bool statics);
+    sph_status enqueue_sort(int kind);
     sph_status enqueue_scan(uint32_t* cnt, uint32_t* out, uint32_t len);
-    sph_status alloc_arrays(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s, uint32_t cap_sq, uint32_t cap_t,
-                            uint32_t max_scenes, uint32_t max_tiles);
+    sph_status alloc_arrays(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s, uint32_t cap_sq, uint32_t cap_sf,
+                            uint32_t cap_t, uint32_t max_scenes, uint32_t max_tiles);
     sph_status enqueue_step_staged(bool record_accel, bool timed);
     sph_status enqueue_step_persistent();
     sph_status ensure_events();
-    SortArgs sort_args(bool statics) const;
+    SortArgs sort_args(int kind) const;
     StepArgs step_args() const;
 
     int device_ = 0;
@@ -135,10 +145,10 @@ private:
     cudaEvent_t events_[6] = {};
     float stage_ms_[5] = {};
     uint32_t persistent_ctas_ = 0;
-    uint32_t cap_n_ = 0, cap_q_ = 0, cap_s_ = 0, cap_sq_ = 0, cap_t_ = 0, max_scenes_ = 0, max_tiles_ = 0;
+    uint32_t cap_n_ = 0, cap_q_ = 0, cap_s_ = 0, cap_sq_ = 0, cap_sf_ = 0, cap_t_ = 0, max_scenes_ = 0, max_tiles_ = 0;
     std::vector<uint32_t> tile_first_;     // first tile of each scene
     Tile* d_tmp_tiles_ = nullptr;          // tiles of a scene being admitted
-    SceneDesc* d_tmp_scene_ = nullptr;     // its dynamic and static views
+    SceneDesc* d_tmp_scene_ = nullptr;     // its dynamic and two static views
 };
 
 }  // namespace sph

@@ -46,16 +46,31 @@ __global__ void __launch_bounds__(kTileThreads) k_gather(SortArgs a)
                 a.pos_dst, a.vel_dst, a.err);
 }
 
+__device__ __forceinline__ NbrArgs nbr_args(const StepArgs& a)
+{
+    return NbrArgs{a.nbr, a.snbr, a.ncount, a.tile_overflow, a.nbr_stride};
+}
+
 __global__ void __launch_bounds__(kTileThreads) k_density(StepArgs a)
 {
-    density_tile(a.tiles[blockIdx.x], a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart);
+    density_tile(blockIdx.x, a.tiles[blockIdx.x], a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart, nbr_args(a));
 }
 
 template <bool kRecord>
 __global__ void __launch_bounds__(kTileThreads) k_force(StepArgs a)
 {
-    force_tile<kRecord>(a.tiles[blockIdx.x], a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart, a.tris,
-                        a.pos_tmp, a.vel_tmp, a.key, a.arrival, a.count, a.accel);
+    force_tile<kRecord>(a.tiles[blockIdx.x], a.scenes, a.pos, a.vel, a.spos, a.tris, nbr_args(a), a.pos_tmp, a.vel_tmp,
+                        a.key, a.arrival, a.count, a.accel);
+}
+
+// Particles whose neighbour list overflowed; whole tiles without one exit at
+// once (the density pass records a per-tile flag).
+template <bool kRecord>
+__global__ void __launch_bounds__(kTileThreads) k_force_overflow(StepArgs a)
+{
+    if (a.tile_overflow[blockIdx.x] == 0u) return;
+    force_overflow_tile<kRecord>(a.tiles[blockIdx.x], a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart, a.tris,
+                                 nbr_args(a), a.pos_tmp, a.vel_tmp, a.key, a.arrival, a.count, a.accel);
 }
 
 // Bounded grid barrier for the persistent kernel (all CTAs co-resident by
@@ -94,12 +109,17 @@ __global__ void __launch_bounds__(kTileThreads) k_step_persistent(StepArgs a, ui
     // tile status so this step's look-back starts from empty
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < scan_tiles; t += gridDim.x * blockDim.x)
         a.scan_status[t] = 0ull;
+    const NbrArgs nl = nbr_args(a);
     for (uint32_t t = blockIdx.x; t < a.num_tiles; t += gridDim.x)
-        density_tile(a.tiles[t], a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart);
+        density_tile(t, a.tiles[t], a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart, nl);
     grid_barrier(a.bar_count, a.bar_gen, a.err);
-    for (uint32_t t = blockIdx.x; t < a.num_tiles; t += gridDim.x)
-        force_tile<false>(a.tiles[t], a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart, a.tris, a.pos_tmp,
-                          a.vel_tmp, a.key, a.arrival, a.count, a.accel);
+    for (uint32_t t = blockIdx.x; t < a.num_tiles; t += gridDim.x) {
+        force_tile<false>(a.tiles[t], a.scenes, a.pos, a.vel, a.spos, a.tris, nl, a.pos_tmp, a.vel_tmp, a.key,
+                          a.arrival, a.count, a.accel);
+        if (a.tile_overflow[t])
+            force_overflow_tile<false>(a.tiles[t], a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart, a.tris, nl,
+                                       a.pos_tmp, a.vel_tmp, a.key, a.arrival, a.count, a.accel);
+    }
     grid_barrier(a.bar_count, a.bar_gen, a.err);
     for (uint32_t t = blockIdx.x; t < scan_tiles; t += gridDim.x)
         scan_tile(t, a.count, a.start, a.scan_len, a.scan_status, a.err, sm);
@@ -135,8 +155,11 @@ __global__ void __launch_bounds__(kTileThreads) k_unsort(const Tile* tiles, cons
 
 // Upload staging (caller's order, positions and velocities as float4 pairs)
 // -> unsorted tmp arrays with the input index in pos.w.
+// Dynamic particles carry their input index in w; static particles carry
+// the Morton code of their cell, which the neighbour passes compare against
+// the cell being visited.
 __global__ void __launch_bounds__(kTileThreads) k_load(const Tile* tiles, const SceneDesc* scenes, const float4* in,
-                                                       float4* pos_tmp, float4* vel_tmp)
+                                                       float4* pos_tmp, float4* vel_tmp, int statics)
 {
     const Tile tile = tiles[blockIdx.x];
     const SceneDesc& sc = scenes[tile.scene];
@@ -144,7 +167,8 @@ __global__ void __launch_bounds__(kTileThreads) k_load(const Tile* tiles, const 
     if (i >= tile.end) return;
     const float4 p = in[2 * (size_t)i];
     const float4 v = in[2 * (size_t)i + 1];
-    pos_tmp[i] = make_float4(p.x, p.y, p.z, __uint_as_float(i - sc.p_off));
+    const uint32_t w = statics ? cell_hash(p.x, p.y, p.z, sc.h) : i - sc.p_off;
+    pos_tmp[i] = make_float4(p.x, p.y, p.z, __uint_as_float(w));
     vel_tmp[i] = make_float4(v.x, v.y, v.z, 0.f);
 }
 
@@ -180,12 +204,14 @@ StepState::~StepState() { release(); }
 void StepState::release()
 {
     if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
-    void* ptrs[] = {d_scenes, d_sscenes, d_tiles, d_stiles, pos, vel, pos_tmp, vel_tmp, key, arrival, perm, count,
-                    start, scan_status, scan_ticket, err, bar, spos, sstart, tris, accel, accel_io, staging,
-                    d_tmp_tiles_, d_tmp_scene_};
+    void* ptrs[] = {d_scenes, d_sscenes, d_sfscenes, d_tiles, d_stiles, pos, vel, pos_tmp, vel_tmp, key, arrival,
+                    perm, count, start, scan_status, scan_ticket, err, bar, spos, sstart, spos_ref, sstart_ref, tris,
+                    accel, accel_io, staging, d_tmp_tiles_, d_tmp_scene_, nbr, snbr, ncount, tile_overflow};
     for (void* p : ptrs)
         if (p) cudaFree(p);
-    d_scenes = d_sscenes = d_tmp_scene_ = nullptr;
+    d_scenes = d_sscenes = d_sfscenes = d_tmp_scene_ = nullptr;
+    spos_ref = nullptr;
+    sstart_ref = nbr = snbr = ncount = tile_overflow = nullptr;
     d_tiles = d_stiles = d_tmp_tiles_ = nullptr;
     pos = vel = pos_tmp = vel_tmp = spos = accel = accel_io = nullptr;
     staging = nullptr;
@@ -200,8 +226,8 @@ void StepState::release()
     stiles.clear();
     tile_first_.clear();
     total_n = total_s = total_t = 0;
-    scan_len = sscan_len = 0;
-    cap_n_ = cap_q_ = cap_s_ = cap_sq_ = cap_t_ = max_scenes_ = max_tiles_ = 0;
+    scan_len = sscan_len = sfscan_len = 0;
+    cap_n_ = cap_q_ = cap_s_ = cap_sq_ = cap_sf_ = cap_t_ = max_scenes_ = max_tiles_ = 0;
 }
 
 static SceneDesc make_scene_desc(const sph_params& p, float dt)
@@ -231,18 +257,21 @@ SceneDesc scene_desc_for(const SceneInput& in)
     d.t = in.t;
     d.fm_b = make_fastmod(d.buckets);
     d.fm_s = make_fastmod(in.s);
+    d.sf_buckets = fast_static_buckets(in.s);
+    d.fm_sf = make_fastmod(d.sf_buckets);
     return d;
 }
 
-static SceneDesc static_view(SceneDesc d)
+// The same scene with a static index space in the dynamic fields, so the
+// sort kernels serve both particle kinds: the reference's s-bucket table
+// (fast = false) or the neighbour-pass table (fast = true).
+static SceneDesc static_view(SceneDesc d, bool fast)
 {
-    // the same scene with the static index spaces in the dynamic fields, so
-    // the sort kernels serve both particle kinds
     d.p_off = d.s_off;
     d.n = d.s;
-    d.q_off = d.sq_off;
-    d.buckets = d.s;
-    d.fm_b = d.fm_s;
+    d.q_off = fast ? d.sf_off : d.sq_off;
+    d.buckets = fast ? d.sf_buckets : d.s;
+    d.fm_b = fast ? d.fm_sf : d.fm_s;
     return d;
 }
 
@@ -271,27 +300,29 @@ static uint32_t tiles_for(uint32_t n) { return (n + kTileThreads - 1) / kTileThr
 
 // Allocates every device array for the given capacities (all zero-filled
 // where the algorithm needs zeros: bucket counters, scan status, errors).
-sph_status StepState::alloc_arrays(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s, uint32_t cap_sq, uint32_t cap_t,
-                                   uint32_t max_scenes, uint32_t max_tiles)
+sph_status StepState::alloc_arrays(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s, uint32_t cap_sq, uint32_t cap_sf,
+                                   uint32_t cap_t, uint32_t max_scenes, uint32_t max_tiles)
 {
     cap_n_ = cap_n;
     cap_q_ = cap_q;
     cap_s_ = cap_s;
     cap_sq_ = cap_sq;
+    cap_sf_ = cap_sf;
     cap_t_ = cap_t;
     max_scenes_ = std::max<uint32_t>(1, max_scenes);
     max_tiles_ = std::max<uint32_t>(1, max_tiles);
     const uint32_t work_n = std::max(cap_n, cap_s);
-    const uint32_t cnt_len = std::max(cap_q, cap_sq) + 1u;
+    const uint32_t cnt_len = std::max(std::max(cap_q, cap_sq), cap_sf) + 1u;
     const uint32_t scan_tiles_max = (cnt_len + kScanTile - 1) / kScanTile;
     sph_status st;
 #define ALLOC(ptr, cnt) if ((st = dev_alloc(&(ptr), (cnt))) != SPH_OK) return st
     ALLOC(d_scenes, max_scenes_);
     ALLOC(d_sscenes, max_scenes_);
+    ALLOC(d_sfscenes, max_scenes_);
     ALLOC(d_tiles, max_tiles_);
     ALLOC(d_stiles, max_tiles_);
     ALLOC(d_tmp_tiles_, tiles_for(work_n) + 1);
-    ALLOC(d_tmp_scene_, 2);
+    ALLOC(d_tmp_scene_, 3);
     ALLOC(pos, cap_n);
     ALLOC(vel, cap_n);
     ALLOC(pos_tmp, work_n);
@@ -306,7 +337,13 @@ sph_status StepState::alloc_arrays(uint32_t cap_n, uint32_t cap_q, uint32_t cap_
     ALLOC(err, 1);
     ALLOC(bar, 2);
     ALLOC(spos, cap_s);
-    ALLOC(sstart, cap_sq + 1ull);
+    ALLOC(sstart, cap_sf + 1ull);
+    ALLOC(spos_ref, cap_s);
+    ALLOC(sstart_ref, cap_sq + 1ull);
+    ALLOC(nbr, (size_t)kMaxNbr * cap_n);
+    ALLOC(snbr, (size_t)kMaxSNbr * cap_n);
+    ALLOC(ncount, cap_n);
+    ALLOC(tile_overflow, max_tiles_);
     ALLOC(tris, 9ull * cap_t);
     ALLOC(staging, 2ull * work_n);
 #undef ALLOC
@@ -344,7 +381,7 @@ sph_status StepState::build(int device, cudaStream_t stream, const std::vector<S
     release();
     device_ = device;
     stream_ = stream;
-    uint64_t p_off = 0, q_off = 0, s_off = 0, sq_off = 0, t_off = 0;
+    uint64_t p_off = 0, q_off = 0, s_off = 0, sq_off = 0, sf_off = 0, t_off = 0;
     for (size_t k = 0; k < inputs.size(); ++k) {
         const SceneInput& in = inputs[k];
         sph_status st = validate_scene(in);
@@ -354,6 +391,7 @@ sph_status StepState::build(int device, cudaStream_t stream, const std::vector<S
         d.q_off = (uint32_t)q_off;
         d.s_off = (uint32_t)s_off;
         d.sq_off = (uint32_t)sq_off;
+        d.sf_off = (uint32_t)sf_off;
         d.t_off = (uint32_t)t_off;
         scenes.push_back(d);
         tile_first_.push_back((uint32_t)tiles.size());
@@ -365,8 +403,9 @@ sph_status StepState::build(int device, cudaStream_t stream, const std::vector<S
         q_off += d.buckets;
         s_off += in.s;
         sq_off += in.s;
+        sf_off += d.sf_buckets;
         t_off += in.t;
-        if (p_off > kMaxParticles || s_off > kMaxParticles || q_off >= (1ull << 31)) {
+        if (p_off > kMaxParticles || s_off > kMaxParticles || q_off >= (1ull << 31) || sf_off >= (1ull << 31)) {
             set_last_error("total particle or bucket count exceeds the 32-bit index space");
             return SPH_ERR_CAPACITY;
         }
@@ -376,11 +415,16 @@ sph_status StepState::build(int device, cudaStream_t stream, const std::vector<S
     total_t = (uint32_t)t_off;
     scan_len = (uint32_t)q_off + 1u;
     sscan_len = (uint32_t)sq_off + 1u;
-    sph_status st = alloc_arrays(total_n, (uint32_t)q_off, total_s, (uint32_t)sq_off, total_t, (uint32_t)scenes.size(),
-                                 (uint32_t)std::max(tiles.size(), stiles.size()));
+    sfscan_len = (uint32_t)sf_off + 1u;
+    sph_status st = alloc_arrays(total_n, (uint32_t)q_off, total_s, (uint32_t)sq_off, (uint32_t)sf_off, total_t,
+                                 (uint32_t)scenes.size(), (uint32_t)std::max(tiles.size(), stiles.size()));
     if (st != SPH_OK) return st;
-    std::vector<SceneDesc> sview;
-    for (const auto& d : scenes) sview.push_back(static_view(d));
+    std::vector<SceneDesc> sview, sfview;
+    for (const auto& d : scenes) {
+        sview.push_back(static_view(d, false));
+        sfview.push_back(static_view(d, true));
+    }
+    CUDA_TRY(cudaMemcpyAsync(d_sfscenes, sfview.data(), sizeof(SceneDesc) * sfview.size(), cudaMemcpyHostToDevice, stream_));
     CUDA_TRY(cudaMemcpyAsync(d_scenes, scenes.data(), sizeof(SceneDesc) * scenes.size(), cudaMemcpyHostToDevice, stream_));
     CUDA_TRY(cudaMemcpyAsync(d_sscenes, sview.data(), sizeof(SceneDesc) * sview.size(), cudaMemcpyHostToDevice, stream_));
     if (!tiles.empty())
@@ -399,7 +443,8 @@ sph_status StepState::build(int device, cudaStream_t stream, const std::vector<S
     }
     if (total_s) {
         if ((st = enqueue_load(staging, /*statics=*/true)) != SPH_OK) return st;
-        if ((st = enqueue_sort(/*statics=*/true)) != SPH_OK) return st;
+        if ((st = enqueue_sort(1)) != SPH_OK) return st;
+        if ((st = enqueue_sort(2)) != SPH_OK) return st;
         CUDA_TRY(cudaStreamSynchronize(stream_));
     }
     for (size_t k = 0; k < inputs.size(); ++k)
@@ -407,7 +452,7 @@ sph_status StepState::build(int device, cudaStream_t stream, const std::vector<S
             return st;
     if (total_n) {
         if ((st = enqueue_load(staging, false)) != SPH_OK) return st;
-        if ((st = enqueue_sort(false)) != SPH_OK) return st;
+        if ((st = enqueue_sort(0)) != SPH_OK) return st;
     }
     CUDA_TRY(cudaStreamSynchronize(stream_));
     return check_device_error();
@@ -416,12 +461,12 @@ sph_status StepState::build(int device, cudaStream_t stream, const std::vector<S
 // ---- arena mode ---------------------------------------------------------------
 
 sph_status StepState::init_arena(int device, cudaStream_t stream, uint32_t cap_n, uint32_t cap_q, uint32_t cap_s,
-                                 uint32_t cap_sq, uint32_t max_scenes)
+                                 uint32_t cap_sq, uint32_t cap_sf, uint32_t max_scenes)
 {
     release();
     device_ = device;
     stream_ = stream;
-    return alloc_arrays(cap_n, cap_q, cap_s, cap_sq, 0, max_scenes, tiles_for(cap_n) + max_scenes);
+    return alloc_arrays(cap_n, cap_q, cap_s, cap_sq, cap_sf, 0, max_scenes, tiles_for(cap_n) + max_scenes);
 }
 
 template <typename T>
@@ -440,16 +485,18 @@ static sph_status grow_one(T** p, size_t old_count, size_t new_count, bool zero_
     return SPH_OK;
 }
 
-sph_status StepState::grow_arena(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s, uint32_t cap_sq)
+sph_status StepState::grow_arena(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s, uint32_t cap_sq, uint32_t cap_sf)
 {
     cap_n = std::max(cap_n, cap_n_);
     cap_q = std::max(cap_q, cap_q_);
     cap_s = std::max(cap_s, cap_s_);
     cap_sq = std::max(cap_sq, cap_sq_);
-    if (cap_n == cap_n_ && cap_q == cap_q_ && cap_s == cap_s_ && cap_sq == cap_sq_) return SPH_OK;
+    cap_sf = std::max(cap_sf, cap_sf_);
+    if (cap_n == cap_n_ && cap_q == cap_q_ && cap_s == cap_s_ && cap_sq == cap_sq_ && cap_sf == cap_sf_) return SPH_OK;
     if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
     const size_t old_work = std::max(cap_n_, cap_s_), new_work = std::max(cap_n, cap_s);
-    const size_t old_cnt = std::max(cap_q_, cap_sq_) + 1ull, new_cnt = std::max(cap_q, cap_sq) + 1ull;
+    const size_t old_cnt = std::max(std::max(cap_q_, cap_sq_), cap_sf_) + 1ull;
+    const size_t new_cnt = std::max(std::max(cap_q, cap_sq), cap_sf) + 1ull;
     const size_t new_scan_tiles = (new_cnt + kScanTile - 1) / kScanTile;
     sph_status st;
 #define GROW(ptr, o, nw, z) if ((st = grow_one(&(ptr), (o), (nw), (z), stream_)) != SPH_OK) return st
@@ -464,7 +511,13 @@ sph_status StepState::grow_arena(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s,
     GROW(count, old_cnt, new_cnt, true);
     GROW(start, cap_q_ + 1ull, cap_q + 1ull, false);
     GROW(spos, cap_s_, cap_s, false);
-    GROW(sstart, cap_sq_ + 1ull, cap_sq + 1ull, false);
+    GROW(sstart, cap_sf_ + 1ull, cap_sf + 1ull, false);
+    GROW(spos_ref, cap_s_, cap_s, false);
+    GROW(sstart_ref, cap_sq_ + 1ull, cap_sq + 1ull, false);
+    GROW(nbr, 0, (size_t)kMaxNbr * cap_n, false);
+    GROW(snbr, 0, (size_t)kMaxSNbr * cap_n, false);
+    GROW(ncount, 0, cap_n, false);
+    GROW(tile_overflow, 0, tiles_for(cap_n) + max_scenes_, false);
     GROW(scan_status, 0, new_scan_tiles, true);
     GROW(d_tmp_tiles_, 0, tiles_for((uint32_t)new_work) + 1, false);
     GROW(d_tiles, 0, tiles_for(cap_n) + max_scenes_, false);
@@ -477,6 +530,7 @@ sph_status StepState::grow_arena(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s,
     cap_q_ = cap_q;
     cap_s_ = cap_s;
     cap_sq_ = cap_sq;
+    cap_sf_ = cap_sf;
     return set_active(scenes);
 }
 
@@ -485,47 +539,43 @@ sph_status StepState::grow_arena(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s,
 // (a sub-range scan yields local starts; the per-scene delta absorbs that).
 sph_status StepState::admit_scene(const SceneDesc& d, const SceneInput& in)
 {
-    if (d.p_off + (uint64_t)d.n > cap_n_ || d.q_off + (uint64_t)d.buckets + 1 > cap_q_ + 1ull ||
-        d.s_off + (uint64_t)d.s > cap_s_ || d.sq_off + (uint64_t)d.s + 1 > cap_sq_ + 1ull) {
+    if (d.p_off + (uint64_t)d.n > cap_n_ || d.q_off + (uint64_t)d.buckets > cap_q_ ||
+        d.s_off + (uint64_t)d.s > cap_s_ || d.sq_off + (uint64_t)d.s > cap_sq_ ||
+        d.sf_off + (uint64_t)d.sf_buckets > cap_sf_) {
         set_last_error("scene ranges exceed the arena");
         return SPH_ERR_CAPACITY;
     }
-    if ((d.q_off & 3u) || (d.sq_off & 3u)) {
+    if ((d.q_off & 3u) || (d.sq_off & 3u) || (d.sf_off & 3u)) {
         set_last_error("bucket ranges must start on a multiple of 4");
         return SPH_ERR_INVALID_ARGUMENT;
     }
-    SceneDesc views[2] = {d, static_view(d)};
+    // views: 0 dynamic, 1 statics by the reference's table, 2 by the
+    // neighbour-pass table
+    SceneDesc views[3] = {d, static_view(d, false), static_view(d, true)};
     CUDA_TRY(cudaMemcpyAsync(d_tmp_scene_, views, sizeof(views), cudaMemcpyHostToDevice, stream_));
     std::vector<Tile> tl;
     sph_status st;
-    for (int kind = 1; kind >= 0; --kind) {            // statics first, then dynamics
+    for (int kind : {1, 2, 0}) {
         const SceneDesc& v = views[kind];
         if (!v.n) continue;
         tl.clear();
         for (uint32_t b = 0; b < v.n; b += kTileThreads)
             tl.push_back(Tile{(uint32_t)kind, v.p_off + b, v.p_off + std::min<uint32_t>(b + kTileThreads, v.n), 0});
         CUDA_TRY(cudaMemcpyAsync(d_tmp_tiles_, tl.data(), sizeof(Tile) * tl.size(), cudaMemcpyHostToDevice, stream_));
-        if (kind == 1) {
-            if ((st = upload_particles(stream_, staging, v.p_off, in.spos, nullptr, v.n)) != SPH_OK) return st;
-        } else {
-            if ((st = upload_particles(stream_, staging, v.p_off, in.pos, in.vel, v.n)) != SPH_OK) return st;
-        }
         const unsigned nt = (unsigned)tl.size();
-        k_load<<<nt, kTileThreads, 0, stream_>>>(d_tmp_tiles_, d_tmp_scene_, staging, pos_tmp, vel_tmp);
-        CUDA_TRY(cudaGetLastError());
-        SortArgs a{};
+        if (kind != 2) {   // the second static sort reuses the first one's loaded particles
+            if (kind == 1) {
+                if ((st = upload_particles(stream_, staging, v.p_off, in.spos, nullptr, v.n)) != SPH_OK) return st;
+            } else {
+                if ((st = upload_particles(stream_, staging, v.p_off, in.pos, in.vel, v.n)) != SPH_OK) return st;
+            }
+            k_load<<<nt, kTileThreads, 0, stream_>>>(d_tmp_tiles_, d_tmp_scene_, staging, pos_tmp, vel_tmp,
+                                                     kind != 0 ? 1 : 0);
+            CUDA_TRY(cudaGetLastError());
+        }
+        SortArgs a = sort_args(kind);
         a.tiles = d_tmp_tiles_;
         a.scenes = d_tmp_scene_;
-        a.pos_src = pos_tmp;
-        a.vel_src = vel_tmp;
-        a.pos_dst = kind ? spos : pos;
-        a.vel_dst = kind ? staging : vel;
-        a.key = key;
-        a.arrival = arrival;
-        a.perm = perm;
-        a.count = count;
-        a.start = kind ? sstart : start;
-        a.err = err;
         k_hash_count<<<nt, kTileThreads, 0, stream_>>>(a);
         CUDA_TRY(cudaGetLastError());
         if ((st = enqueue_scan(count + v.q_off, a.start + v.q_off, v.buckets + 1u)) != SPH_OK) return st;
@@ -578,37 +628,38 @@ sph_status StepState::enqueue_load(const float4* src, bool statics)
     const std::vector<Tile>& tl = statics ? stiles : tiles;
     if (tl.empty()) return SPH_OK;
     k_load<<<(unsigned)tl.size(), kTileThreads, 0, stream_>>>(statics ? d_stiles : d_tiles, statics ? d_sscenes : d_scenes,
-                                                                src, pos_tmp, vel_tmp);
+                                                                src, pos_tmp, vel_tmp, statics ? 1 : 0);
     CUDA_TRY(cudaGetLastError());
     return SPH_OK;
 }
 
-SortArgs StepState::sort_args(bool statics) const
+SortArgs StepState::sort_args(int kind) const
 {
     SortArgs a{};
-    a.tiles = statics ? d_stiles : d_tiles;
-    a.scenes = statics ? d_sscenes : d_scenes;
+    a.tiles = kind == 0 ? d_tiles : d_stiles;
+    a.scenes = kind == 0 ? d_scenes : (kind == 1 ? d_sscenes : d_sfscenes);
     a.pos_src = pos_tmp;
     a.vel_src = vel_tmp;
-    a.pos_dst = statics ? spos : pos;
-    a.vel_dst = statics ? staging : vel;   // static velocities are discarded
+    a.pos_dst = kind == 0 ? pos : (kind == 1 ? spos_ref : spos);
+    a.vel_dst = kind == 0 ? vel : staging;   // static velocities are discarded
     a.key = key;
     a.arrival = arrival;
     a.perm = perm;
     a.count = count;
-    a.start = statics ? sstart : start;
+    a.start = kind == 0 ? start : (kind == 1 ? sstart_ref : sstart);
     a.err = err;
     return a;
 }
 
-// Counting sort of the tmp arrays into the sorted state: hash + count, scan,
-// scatter, stable gather (positions must already be in pos_tmp).
-sph_status StepState::enqueue_sort(bool statics)
+// Counting sort of the tmp arrays into a sorted array: hash + count, scan,
+// scatter, stable gather (positions must already be in pos_tmp, and stay
+// there, so both static sorts read the same load).
+sph_status StepState::enqueue_sort(int kind)
 {
-    const std::vector<Tile>& tl = statics ? stiles : tiles;
+    const std::vector<Tile>& tl = kind == 0 ? tiles : stiles;
     if (tl.empty()) return SPH_OK;
-    SortArgs a = sort_args(statics);
-    const uint32_t len = statics ? sscan_len : scan_len;
+    SortArgs a = sort_args(kind);
+    const uint32_t len = kind == 0 ? scan_len : (kind == 1 ? sscan_len : sfscan_len);
     const unsigned nt = (unsigned)tl.size();
     k_hash_count<<<nt, kTileThreads, 0, stream_>>>(a);
     CUDA_TRY(cudaGetLastError());
@@ -656,6 +707,11 @@ StepArgs StepState::step_args() const
     a.err = err;
     a.bar_count = bar;
     a.bar_gen = bar + 1;
+    a.nbr = nbr;
+    a.snbr = snbr;
+    a.ncount = ncount;
+    a.tile_overflow = tile_overflow;
+    a.nbr_stride = cap_n_;
     return a;
 }
 
@@ -673,15 +729,18 @@ sph_status StepState::enqueue_step_staged(bool record_accel, bool timed)
     if (tiles.empty()) return SPH_OK;
     const unsigned nt = (unsigned)tiles.size();
     StepArgs a = step_args();
-    SortArgs s = sort_args(false);
+    SortArgs s = sort_args(0);
     if (timed) CUDA_TRY(cudaEventRecord(events_[0], stream_));
     k_density<<<nt, kTileThreads, 0, stream_>>>(a);
     CUDA_TRY(cudaGetLastError());
     if (timed) CUDA_TRY(cudaEventRecord(events_[1], stream_));
-    if (record_accel)
+    if (record_accel) {
         k_force<true><<<nt, kTileThreads, 0, stream_>>>(a);
-    else
+        k_force_overflow<true><<<nt, kTileThreads, 0, stream_>>>(a);
+    } else {
         k_force<false><<<nt, kTileThreads, 0, stream_>>>(a);
+        k_force_overflow<false><<<nt, kTileThreads, 0, stream_>>>(a);
+    }
     CUDA_TRY(cudaGetLastError());
     if (timed) CUDA_TRY(cudaEventRecord(events_[2], stream_));
     sph_status st = enqueue_scan(count, start, scan_len);
@@ -849,7 +908,7 @@ sph_status StepState::write_scene(uint32_t scene, const sph_dynamic_particle* in
     CUDA_TRY(cudaMemcpyAsync(staging + 2ull * d.p_off, in, sizeof(sph_dynamic_particle) * d.n, cudaMemcpyHostToDevice, stream_));
     sph_status st = enqueue_load(staging, false);
     if (st != SPH_OK) return st;
-    st = enqueue_sort(false);
+    st = enqueue_sort(0);
     if (st != SPH_OK) return st;
     CUDA_TRY(cudaStreamSynchronize(stream_));
     return check_device_error();
@@ -861,14 +920,14 @@ sph_status StepState::read_static(uint32_t scene, sph_static_particle* out, uint
     const SceneDesc& d = scenes[scene];
     if (!d.s) return SPH_OK;
     if (out) {
-        CUDA_TRY(cudaMemcpyAsync(out, spos + d.s_off, sizeof(float4) * d.s, cudaMemcpyDeviceToHost, stream_));
+        CUDA_TRY(cudaMemcpyAsync(out, spos_ref + d.s_off, sizeof(float4) * d.s, cudaMemcpyDeviceToHost, stream_));
     }
     CUDA_TRY(cudaStreamSynchronize(stream_));
     if (out) {
         for (uint32_t i = 0; i < d.s; ++i) out[i].pressure = 0.f;   // static pressure is never written
     }
     if (bucket_starts) {
-        CUDA_TRY(cudaMemcpy(bucket_starts, sstart + d.sq_off, sizeof(uint32_t) * (d.s + 1ull), cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(bucket_starts, sstart_ref + d.sq_off, sizeof(uint32_t) * (d.s + 1ull), cudaMemcpyDeviceToHost));
         const uint32_t b0 = bucket_starts[0];
         for (uint32_t k = 0; k <= d.s; ++k) bucket_starts[k] -= b0;
     }
