@@ -20,6 +20,20 @@
 namespace sph {
 
 constexpr int kTileThreads = 128;          // slots per tile = threads per CTA
+
+// Tuning knobs (compile-time; the defaults are the measured best on GB300).
+// Minimum resident CTAs per SM requested from the register allocator for the
+// two neighbour passes, and how many neighbours one round of the force and
+// density-sum loops loads at once.
+#ifndef SPH_DENSITY_MIN_CTAS
+#define SPH_DENSITY_MIN_CTAS 8
+#endif
+#ifndef SPH_FORCE_MIN_CTAS
+#define SPH_FORCE_MIN_CTAS 6
+#endif
+#ifndef SPH_NBR_BATCH
+#define SPH_NBR_BATCH 4
+#endif
 constexpr int kScanThreads = kTileThreads;  // the scan runs inside the fused kernel too
 constexpr int kScanItems = 16;             // per thread
 constexpr int kScanTile = kScanThreads * kScanItems;
@@ -495,92 +509,145 @@ __device__ __forceinline__ float w0_of(float r2, float h)
     return r < h ? __fmul_rn(__fmul_rn(w, w), w) : 0.f;
 }
 
-__device__ __forceinline__ void density_tile(uint32_t tile_index, const Tile& tile, const SceneDesc* scenes,
-                                             const float4* __restrict__ pos,
-                                             float4* __restrict__ vel, const uint32_t* __restrict__ start,
-                                             const float4* __restrict__ spos, const uint32_t* __restrict__ sstart,
-                                             const NbrArgs& nl)
+// Squared distances from q to the NH home particles, bit-identical to dist2().
+template <int NH>
+struct HomeCoords {
+    float4 p[NH];
+};
+
+template <int NH>
+__device__ __forceinline__ void dist2_n(const float4& q, const HomeCoords<NH>& hc, float (&r2)[NH])
 {
-    const SceneDesc& sc = scenes[tile.scene];
-    const uint32_t i = tile.begin + threadIdx.x;
-    bool overflow = false;
-    if (i < tile.end) {
-        const float h = sc.h, h2 = sc.h2;
-        const float cull2 = __fmul_rn(h2, 1.0001f);
-        const float4 p = pos[i];
-        const Neighbourhood nb = neighbourhood(p.x, p.y, p.z, h);
-        const CellBox box = cell_box(p, h);
-        const uint32_t span = nb_span(nb);
-        const bool cull_d = box.ok && span < sc.buckets;
-        const bool dup_s = span >= sc.s;     // reference static buckets may repeat
-        const uint32_t delta = sc.p_off - __ldg(start + sc.q_off);
-        const uint32_t sdelta = sc.s ? sc.s_off - __ldg(sstart + sc.sf_off) : 0u;
-        const uint32_t stride = nl.stride;
-        uint32_t cnt = 0, scnt = 0;
+#pragma unroll
+    for (int k = 0; k < NH; ++k) r2[k] = dist2(q, hc.p[k]);
+}
+
+// The density pass for NH home particles of one cell.  Every candidate is
+// loaded once for all homes; each home gets its own list, sums, counts and
+// pressure, identical to what it would get alone.  The step uses NH = 1: on
+// GB300 two homes per thread (with packed FP32x2 arithmetic) measured 3x
+// slower, the extra registers costing more occupancy than the shared loads
+// saved.
+template <int NH>
+__device__ __forceinline__ void density_homes(uint32_t tile_index, const SceneDesc& sc, const uint32_t (&hi)[NH],
+                                              const float4 (&hp)[NH], const float4* __restrict__ pos,
+                                              float4* __restrict__ vel, const uint32_t* __restrict__ start,
+                                              const float4* __restrict__ spos, const uint32_t* __restrict__ sstart,
+                                              const NbrArgs& nl)
+{
+    const float h = sc.h, h2 = sc.h2;
+    const float cull2 = __fmul_rn(h2, 1.0001f);
+    HomeCoords<NH> hc;
+    CellBox box[NH];
+    bool box_ok = true;
+#pragma unroll
+    for (int k = 0; k < NH; ++k) {
+        hc.p[k] = hp[k];
+        box[k] = cell_box(hp[k], h);
+        box_ok = box_ok && box[k].ok;
+    }
+    const Neighbourhood nb = neighbourhood(hp[0].x, hp[0].y, hp[0].z, h);
+    const uint32_t span = nb_span(nb);
+    const bool cull_d = box_ok && span < sc.buckets;
+    const bool dup_s = span >= sc.s;     // reference static buckets may repeat
+    const uint32_t delta = sc.p_off - __ldg(start + sc.q_off);
+    const uint32_t sdelta = sc.s ? sc.s_off - __ldg(sstart + sc.sf_off) : 0u;
+    const uint32_t stride = nl.stride;
+    uint32_t cnt[NH], scnt[NH];
+#pragma unroll
+    for (int k = 0; k < NH; ++k) cnt[k] = scnt[k] = 0;
 #pragma unroll 1
-        for (int a = 0; a < 3; ++a)
+    for (int a = 0; a < 3; ++a)
 #pragma unroll 1
-            for (int b = 0; b < 3; ++b)
+        for (int b = 0; b < 3; ++b)
 #pragma unroll 1
-                for (int c = 0; c < 3; ++c) {
-                    const float bd2 = pick3f(a, box.x0, 0.f, box.x2) + pick3f(b, box.y0, 0.f, box.y2) +
-                                      pick3f(c, box.z0, 0.f, box.z2);
-                    const bool far = bd2 > cull2;
-                    const uint32_t hsh = neighbour_hash(nb, a, b, c);
-                    if (!(far && cull_d)) {
-                        const uint32_t bk = sc.q_off + fast_mod(hsh, sc.fm_b);
-                        const uint32_t beg = max(__ldg(start + bk) + delta, sc.p_off);
-                        const uint32_t end = min(__ldg(start + bk + 1) + delta, sc.p_off + sc.n);
-                        for (uint32_t j = beg; j < end; ++j) {
-                            const float4 q = __ldg(pos + j);
-                            if (dist2(q, p) <= h2 && j != i) {
-                                if (cnt < kMaxNbr) nl.nbr[(size_t)cnt * stride + i] = j;
-                                ++cnt;
-                            }
-                        }
-                    }
-                    if (sc.s && !(far && box.ok)) {
-                        const uint32_t sb = sc.sf_off + fast_mod(hsh, sc.fm_sf);
-                        const uint32_t sbeg = max(__ldg(sstart + sb) + sdelta, sc.s_off);
-                        const uint32_t send = min(__ldg(sstart + sb + 1) + sdelta, sc.s_off + sc.s);
-                        uint32_t mult = 0;
-                        for (uint32_t j = sbeg; j < send; ++j) {
-                            const float4 q = __ldg(spos + j);
-                            // statics carry their cell's Morton code: only this cell's count
-                            if (__float_as_uint(q.w) == hsh && dist2(q, p) <= h2) {
-                                if (!mult) mult = dup_s ? static_multiplicity(nb, sc.fm_s, hsh) : 1u;
-                                if (scnt < kMaxSNbr) nl.snbr[(size_t)scnt * stride + i] = j | (mult << kMultShift);
-                                ++scnt;
+            for (int c = 0; c < 3; ++c) {
+                bool far = true;
+#pragma unroll
+                for (int k = 0; k < NH; ++k) {
+                    const float bd2 = pick3f(a, box[k].x0, 0.f, box[k].x2) + pick3f(b, box[k].y0, 0.f, box[k].y2) +
+                                      pick3f(c, box[k].z0, 0.f, box[k].z2);
+                    far = far && bd2 > cull2;
+                }
+                const uint32_t hsh = neighbour_hash(nb, a, b, c);
+                if (!(far && cull_d)) {
+                    const uint32_t bk = sc.q_off + fast_mod(hsh, sc.fm_b);
+                    const uint32_t beg = max(__ldg(start + bk) + delta, sc.p_off);
+                    const uint32_t end = min(__ldg(start + bk + 1) + delta, sc.p_off + sc.n);
+                    for (uint32_t j = beg; j < end; ++j) {
+                        float r2[NH];
+                        dist2_n<NH>(__ldg(pos + j), hc, r2);
+#pragma unroll
+                        for (int k = 0; k < NH; ++k) {
+                            if (r2[k] <= h2 && j != hi[k]) {
+                                if (cnt[k] < kMaxNbr) nl.nbr[(size_t)cnt[k] * stride + hi[k]] = j;
+                                ++cnt[k];
                             }
                         }
                     }
                 }
-        float sum_d = 0.f, sum_s = 0.f;
-        if (cnt <= kMaxNbr) {
-            const uint32_t* lp = nl.nbr + i;
-            for (uint32_t k = 0; k < cnt; ++k, lp += stride) {
-                const uint32_t j = *lp;
-                sum_d = __fadd_rn(sum_d, w0_of(dist2(__ldg(pos + j), p), h));
+                if (sc.s && !(far && box_ok)) {
+                    const uint32_t sb = sc.sf_off + fast_mod(hsh, sc.fm_sf);
+                    const uint32_t sbeg = max(__ldg(sstart + sb) + sdelta, sc.s_off);
+                    const uint32_t send = min(__ldg(sstart + sb + 1) + sdelta, sc.s_off + sc.s);
+                    uint32_t mult = 0;
+                    for (uint32_t j = sbeg; j < send; ++j) {
+                        const float4 q = __ldg(spos + j);
+                        // statics carry their cell's Morton code: only this cell's count
+                        if (__float_as_uint(q.w) != hsh) continue;
+                        float r2[NH];
+                        dist2_n<NH>(q, hc, r2);
+#pragma unroll
+                        for (int k = 0; k < NH; ++k) {
+                            if (r2[k] <= h2) {
+                                if (!mult) mult = dup_s ? static_multiplicity(nb, sc.fm_s, hsh) : 1u;
+                                if (scnt[k] < kMaxSNbr)
+                                    nl.snbr[(size_t)scnt[k] * stride + hi[k]] = j | (mult << kMultShift);
+                                ++scnt[k];
+                            }
+                        }
+                    }
+                }
             }
+#pragma unroll
+    for (int k = 0; k < NH; ++k) {
+        const uint32_t i = hi[k];
+        const float4 p = hp[k];
+        float sum_d = 0.f, sum_s = 0.f;
+        if (cnt[k] <= kMaxNbr) {
+            // four neighbours per round: their loads are issued together
+            const uint32_t* lp = nl.nbr + i;
+            uint32_t m = 0;
+            for (; SPH_NBR_BATCH == 4 && m + 4 <= cnt[k]; m += 4, lp += 4 * (size_t)stride) {
+                const uint32_t j0 = lp[0], j1 = lp[stride], j2 = lp[2 * (size_t)stride], j3 = lp[3 * (size_t)stride];
+                const float4 q0 = __ldg(pos + j0), q1 = __ldg(pos + j1), q2 = __ldg(pos + j2), q3 = __ldg(pos + j3);
+                sum_d = __fadd_rn(sum_d, w0_of(dist2(q0, p), h));
+                sum_d = __fadd_rn(sum_d, w0_of(dist2(q1, p), h));
+                sum_d = __fadd_rn(sum_d, w0_of(dist2(q2, p), h));
+                sum_d = __fadd_rn(sum_d, w0_of(dist2(q3, p), h));
+            }
+            for (; m < cnt[k]; ++m, lp += stride)
+                sum_d = __fadd_rn(sum_d, w0_of(dist2(__ldg(pos + *lp), p), h));
         }
-        if (scnt <= kMaxSNbr) {
+        if (scnt[k] <= kMaxSNbr) {
             const uint32_t* lp = nl.snbr + i;
-            for (uint32_t k = 0; k < scnt; ++k, lp += stride) {
+            for (uint32_t m = 0; m < scnt[k]; ++m, lp += stride) {
                 const uint32_t e = *lp;
                 const float w0 = w0_of(dist2(__ldg(spos + (e & kIndexMask)), p), h);
-                for (uint32_t m = e >> kMultShift; m; --m) sum_s = __fadd_rn(sum_s, w0);
+                for (uint32_t r = e >> kMultShift; r; --r) sum_s = __fadd_rn(sum_s, w0);
             }
         }
-        if (cnt > kMaxNbr || scnt > kMaxSNbr) {
-            // overflow: walk the buckets again, summing directly
+        if (cnt[k] > kMaxNbr || scnt[k] > kMaxSNbr) {
+            // overflow: walk the buckets again for this home, summing directly
+            const Neighbourhood nbk = neighbourhood(p.x, p.y, p.z, h);
 #pragma unroll 1
             for (int a = 0; a < 3; ++a)
 #pragma unroll 1
                 for (int b = 0; b < 3; ++b)
 #pragma unroll 1
                     for (int c = 0; c < 3; ++c) {
-                        const uint32_t hsh = neighbour_hash(nb, a, b, c);
-                        if (cnt > kMaxNbr) {
+                        const uint32_t hsh = neighbour_hash(nbk, a, b, c);
+                        if (cnt[k] > kMaxNbr) {
                             const uint32_t bk = sc.q_off + fast_mod(hsh, sc.fm_b);
                             const uint32_t beg = max(__ldg(start + bk) + delta, sc.p_off);
                             const uint32_t end = min(__ldg(start + bk + 1) + delta, sc.p_off + sc.n);
@@ -589,7 +656,7 @@ __device__ __forceinline__ void density_tile(uint32_t tile_index, const Tile& ti
                                 if (r2 <= h2 && j != i) sum_d = __fadd_rn(sum_d, w0_of(r2, h));
                             }
                         }
-                        if (sc.s && scnt > kMaxSNbr) {
+                        if (sc.s && scnt[k] > kMaxSNbr) {
                             const uint32_t sb = sc.sf_off + fast_mod(hsh, sc.fm_sf);
                             const uint32_t sbeg = max(__ldg(sstart + sb) + sdelta, sc.s_off);
                             const uint32_t send = min(__ldg(sstart + sb + 1) + sdelta, sc.s_off + sc.s);
@@ -598,23 +665,38 @@ __device__ __forceinline__ void density_tile(uint32_t tile_index, const Tile& ti
                                 const float4 q = __ldg(spos + j);
                                 const float r2 = dist2(q, p);
                                 if (__float_as_uint(q.w) == hsh && r2 <= h2) {
-                                    if (!mult) mult = dup_s ? static_multiplicity(nb, sc.fm_s, hsh) : 1u;
+                                    if (!mult) mult = dup_s ? static_multiplicity(nbk, sc.fm_s, hsh) : 1u;
                                     const float w0 = w0_of(r2, h);
-                                    for (uint32_t m = mult; m; --m) sum_s = __fadd_rn(sum_s, w0);
+                                    for (uint32_t r = mult; r; --r) sum_s = __fadd_rn(sum_s, w0);
                                 }
                             }
                         }
                     }
-            overflow = true;
+            atomicOr(nl.tile_overflow + tile_index, 1u);   // cleared by the overflow force pass
         }
-        nl.ncount[i] = (cnt > kMaxNbr ? kOverflow : cnt) | ((scnt > kMaxSNbr ? kOverflow : scnt) << 16);
+        nl.ncount[i] = (cnt[k] > kMaxNbr ? kOverflow : cnt[k]) | ((scnt[k] > kMaxSNbr ? kOverflow : scnt[k]) << 16);
         const float rho = __fadd_rn(sc.self_density,
                                     __fmul_rn(__fadd_rn(__fmul_rn(sum_d, sc.mass), __fmul_rn(sum_s, sc.mass)), sc.kc));
         const float pressure = __fmul_rn(sc.gas, __fsub_rn(rho, sc.rho0));
         reinterpret_cast<float*>(vel + i)[3] = pressure;
     }
-    const int any = __syncthreads_or(overflow ? 1 : 0);
-    if (threadIdx.x == 0) nl.tile_overflow[tile_index] = any ? 1u : 0u;
+}
+
+constexpr int kDensityThreads = kTileThreads;   // one home slot per thread
+
+// One tile of the density pass: thread `lane` owns slot tile.begin + lane.
+__device__ __forceinline__ void density_tile(uint32_t tile_index, const Tile& tile, uint32_t lane,
+                                             const SceneDesc* scenes, const float4* __restrict__ pos,
+                                             float4* __restrict__ vel, const uint32_t* __restrict__ start,
+                                             const float4* __restrict__ spos, const uint32_t* __restrict__ sstart,
+                                             const NbrArgs& nl)
+{
+    const SceneDesc& sc = scenes[tile.scene];
+    const uint32_t i = tile.begin + lane;
+    if (i >= tile.end) return;
+    const uint32_t hi[1] = {i};
+    const float4 hp[1] = {pos[i]};
+    density_homes<1>(tile_index, sc, hi, hp, pos, vel, start, spos, sstart, nl);
 }
 
 // ---- stage: force + integrate + rehash -------------------------------------
@@ -742,9 +824,20 @@ __device__ __forceinline__ void force_tile(const Tile& tile, const SceneDesc* sc
             const uint32_t stride = nl.stride;
             PairSums s;
             s.fp = s.fv = s.fs = make_float3(0.f, 0.f, 0.f);
+            // four neighbours per round: eight position/velocity loads in flight
             const uint32_t* lp = nl.nbr + i;
-#pragma unroll 2
-            for (uint32_t k = 0; k < cd; ++k, lp += stride) {
+            uint32_t k = 0;
+            for (; SPH_NBR_BATCH == 4 && k + 4 <= cd; k += 4, lp += 4 * (size_t)stride) {
+                const uint32_t j0 = __ldg(lp), j1 = __ldg(lp + stride), j2 = __ldg(lp + 2 * (size_t)stride),
+                               j3 = __ldg(lp + 3 * (size_t)stride);
+                const float4 q0 = __ldg(pos + j0), q1 = __ldg(pos + j1), q2 = __ldg(pos + j2), q3 = __ldg(pos + j3);
+                const float4 u0 = __ldg(vel + j0), u1 = __ldg(vel + j1), u2 = __ldg(vel + j2), u3 = __ldg(vel + j3);
+                add_dynamic_pair(s, p, v, pi, h, q0, u0);
+                add_dynamic_pair(s, p, v, pi, h, q1, u1);
+                add_dynamic_pair(s, p, v, pi, h, q2, u2);
+                add_dynamic_pair(s, p, v, pi, h, q3, u3);
+            }
+            for (; k < cd; ++k, lp += stride) {
                 const uint32_t j = __ldg(lp);
                 add_dynamic_pair(s, p, v, pi, h, __ldg(pos + j), __ldg(vel + j));
             }

@@ -51,13 +51,14 @@ __device__ __forceinline__ NbrArgs nbr_args(const StepArgs& a)
     return NbrArgs{a.nbr, a.snbr, a.ncount, a.tile_overflow, a.nbr_stride};
 }
 
-__global__ void __launch_bounds__(kTileThreads) k_density(StepArgs a)
+__global__ void __launch_bounds__(kDensityThreads, SPH_DENSITY_MIN_CTAS) k_density(StepArgs a)
 {
-    density_tile(blockIdx.x, a.tiles[blockIdx.x], a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart, nbr_args(a));
+    density_tile(blockIdx.x, a.tiles[blockIdx.x], threadIdx.x, a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart,
+                 nbr_args(a));
 }
 
 template <bool kRecord>
-__global__ void __launch_bounds__(kTileThreads) k_force(StepArgs a)
+__global__ void __launch_bounds__(kTileThreads, SPH_FORCE_MIN_CTAS) k_force(StepArgs a)
 {
     force_tile<kRecord>(a.tiles[blockIdx.x], a.scenes, a.pos, a.vel, a.spos, a.tris, nbr_args(a), a.pos_tmp, a.vel_tmp,
                         a.key, a.arrival, a.count, a.accel);
@@ -71,6 +72,8 @@ __global__ void __launch_bounds__(kTileThreads) k_force_overflow(StepArgs a)
     if (a.tile_overflow[blockIdx.x] == 0u) return;
     force_overflow_tile<kRecord>(a.tiles[blockIdx.x], a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart, a.tris,
                                  nbr_args(a), a.pos_tmp, a.vel_tmp, a.key, a.arrival, a.count, a.accel);
+    __syncthreads();
+    if (threadIdx.x == 0) a.tile_overflow[blockIdx.x] = 0u;   // every thread has read the flag
 }
 
 // Bounded grid barrier for the persistent kernel (all CTAs co-resident by
@@ -111,14 +114,17 @@ __global__ void __launch_bounds__(kTileThreads) k_step_persistent(StepArgs a, ui
         a.scan_status[t] = 0ull;
     const NbrArgs nl = nbr_args(a);
     for (uint32_t t = blockIdx.x; t < a.num_tiles; t += gridDim.x)
-        density_tile(t, a.tiles[t], a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart, nl);
+        density_tile(t, a.tiles[t], threadIdx.x, a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart, nl);
     grid_barrier(a.bar_count, a.bar_gen, a.err);
     for (uint32_t t = blockIdx.x; t < a.num_tiles; t += gridDim.x) {
         force_tile<false>(a.tiles[t], a.scenes, a.pos, a.vel, a.spos, a.tris, nl, a.pos_tmp, a.vel_tmp, a.key,
                           a.arrival, a.count, a.accel);
-        if (a.tile_overflow[t])
+        if (a.tile_overflow[t]) {
             force_overflow_tile<false>(a.tiles[t], a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart, a.tris, nl,
                                        a.pos_tmp, a.vel_tmp, a.key, a.arrival, a.count, a.accel);
+            __syncthreads();
+            if (threadIdx.x == 0) a.tile_overflow[t] = 0u;
+        }
     }
     grid_barrier(a.bar_count, a.bar_gen, a.err);
     for (uint32_t t = blockIdx.x; t < scan_tiles; t += gridDim.x)
@@ -351,6 +357,7 @@ sph_status StepState::alloc_arrays(uint32_t cap_n, uint32_t cap_q, uint32_t cap_
     CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(uint32_t), stream_));
     CUDA_TRY(cudaMemsetAsync(bar, 0, 2 * sizeof(uint32_t), stream_));
     CUDA_TRY(cudaMemsetAsync(scan_status, 0, sizeof(unsigned long long) * scan_tiles_max, stream_));
+    CUDA_TRY(cudaMemsetAsync(tile_overflow, 0, sizeof(uint32_t) * max_tiles_, stream_));
     CUDA_TRY(cudaStreamSynchronize(stream_));
     return SPH_OK;
 }
@@ -517,7 +524,7 @@ sph_status StepState::grow_arena(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s,
     GROW(nbr, 0, (size_t)kMaxNbr * cap_n, false);
     GROW(snbr, 0, (size_t)kMaxSNbr * cap_n, false);
     GROW(ncount, 0, cap_n, false);
-    GROW(tile_overflow, 0, tiles_for(cap_n) + max_scenes_, false);
+    GROW(tile_overflow, 0, tiles_for(cap_n) + max_scenes_, true);
     GROW(scan_status, 0, new_scan_tiles, true);
     GROW(d_tmp_tiles_, 0, tiles_for((uint32_t)new_work) + 1, false);
     GROW(d_tiles, 0, tiles_for(cap_n) + max_scenes_, false);
@@ -731,7 +738,7 @@ sph_status StepState::enqueue_step_staged(bool record_accel, bool timed)
     StepArgs a = step_args();
     SortArgs s = sort_args(0);
     if (timed) CUDA_TRY(cudaEventRecord(events_[0], stream_));
-    k_density<<<nt, kTileThreads, 0, stream_>>>(a);
+    k_density<<<nt, kDensityThreads, 0, stream_>>>(a);
     CUDA_TRY(cudaGetLastError());
     if (timed) CUDA_TRY(cudaEventRecord(events_[1], stream_));
     if (record_accel) {
