@@ -173,6 +173,24 @@ SPH_API sph_status sph_engine_get_stream(sph_engine* engine, void** stream);
 SPH_API sph_status sph_cell_sort(int device, const float* pos, uint32_t n, float h, uint32_t buckets,
                                  uint32_t* keys, uint32_t* counts, uint32_t* starts, uint32_t* order);
 
+/* The same counting sort for callers that cannot allocate device memory
+ * (code under a caller-owned pool or allocator, a frame loop that must not
+ * allocate, a plugin whose host application owns all device memory).  It has
+ * no counterpart in the reference.  Every pointer is a DEVICE pointer owned
+ * by the caller: pos n x 3 floats, keys n, starts buckets+1 (16-byte
+ * aligned), order n; the outputs mean what sph_cell_sort's do.  Work is
+ * queued on `stream` (a cudaStream_t, NULL = default stream) and the call
+ * returns after it finished.  The sort's scratch is a fixed array inside the
+ * library (about 4.2 MiB, held on every GPU that loads the library until the
+ * process exits), so the call makes no allocation; n is limited to 262144 and
+ * buckets to 524288, larger requests fail with SPH_ERR_CAPACITY.  The first
+ * call on a device looks up that array's device address (with the device
+ * current), so make it before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU race and must be serialised by the
+ * caller. */
+SPH_API sph_status sph_cell_sort_noalloc(const float* pos, uint32_t n, float h, uint32_t buckets,
+                                         uint32_t* keys, uint32_t* starts, uint32_t* order, void* stream);
+
 /* ---- batched engine: many scenes advanced by one persistent launch ------ */
 
 typedef struct sph_batch sph_batch;

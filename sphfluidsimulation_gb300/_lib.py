@@ -64,6 +64,7 @@ _SIGS = {
     "sph_engine_kernel_times": (_st, [_vp, _fp, C.c_int]),
     "sph_engine_get_stream": (_st, [_vp, C.POINTER(_vp)]),
     "sph_cell_sort": (_st, [C.c_int, _fp, C.c_uint32, C.c_float, C.c_uint32, _up, _up, _up, _up]),
+    "sph_cell_sort_noalloc": (_st, [_vp, C.c_uint32, C.c_float, C.c_uint32, _vp, _vp, _vp, _vp]),
     "sph_batch_create": (_st, [C.POINTER(_vp), C.c_int]),
     "sph_batch_destroy": (_st, [_vp]),
     "sph_batch_add_scene": (_st, [_vp, C.POINTER(SphParams), _fp, _fp, C.c_uint32, _fp, C.c_uint32, _fp,
