@@ -217,6 +217,15 @@ SPH_API sph_status sph_batch_finalize(sph_batch* batch);
 SPH_API sph_status sph_batch_step(sph_batch* batch, uint32_t steps);
 SPH_API sph_status sph_batch_set_mode(sph_batch* batch, int mode);
 
+/* Autotuner: times trial_steps steps of each configuration -- the staged
+ * step graph, and the persistent kernel at 1, 2, ... CTAs per SM up to its
+ * occupancy limit -- on a saved copy of the state (restored after each
+ * trial, so the simulation does not advance), and keeps the fastest.
+ * Reports the chosen mode (0 persistent, 1 staged), the persistent grid
+ * size (0 when staged) and its time per step (any output may be NULL). */
+SPH_API sph_status sph_batch_autotune(sph_batch* batch, uint32_t trial_steps, int* mode, uint32_t* grid_ctas,
+                                      float* ms_per_step);
+
 /* Reads one scene's particles in its input order. */
 SPH_API sph_status sph_batch_read_scene(sph_batch* batch, uint32_t scene_id, sph_dynamic_particle* out);
 

@@ -72,6 +72,7 @@ _SIGS = {
     "sph_batch_finalize": (_st, [_vp]),
     "sph_batch_step": (_st, [_vp, C.c_uint32]),
     "sph_batch_set_mode": (_st, [_vp, C.c_int]),
+    "sph_batch_autotune": (_st, [_vp, C.c_uint32, C.POINTER(C.c_int), _up, _fp]),
     "sph_batch_read_scene": (_st, [_vp, C.c_uint32, _vp]),
     "sph_batch_info": (_st, [_vp, _u64p, _up, _up]),
     "sph_server_create": (_st, [C.POINTER(_vp), C.c_int, C.c_uint64, C.c_uint32]),

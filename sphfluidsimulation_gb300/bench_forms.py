@@ -31,14 +31,18 @@ def _percentiles(lat: List[float]) -> Dict[str, float]:
             "p99_s": float(np.percentile(a, 99)), "mean_s": float(a.mean())}
 
 
-def run_batched(steps: int, count: int = 96, seed: int = 0, mode: int = 0) -> Dict:
+def run_batched(steps: int, count: int = 96, seed: int = 0, mode: int = -1) -> Dict:
     scs = scenes.batched_scenes(count=count, seed=seed, steps=steps)
     total = sum(sc.n for sc in scs)
     b = Batch()
     for sc in scs:
         b.add_scene(sc)
     b.finalize()
-    b.set_mode(mode)
+    if mode < 0:
+        chosen = b.autotune(3)                  # picks staged graph or persistent grid size
+    else:
+        b.set_mode(mode)
+        chosen = None
     b.step(2)                                   # warm-up
     t0 = time.perf_counter()
     b.step(steps)
@@ -61,7 +65,9 @@ def run_batched(steps: int, count: int = 96, seed: int = 0, mode: int = 0) -> Di
     return {"scenes": count, "particles": total, "steps": steps,
             "batched_particle_steps_per_s": total * steps / tb, "plain_looped_particle_steps_per_s": total * steps / tp,
             "speedup": tp / tb, "batched_ms_per_step": 1e3 * tb / steps, "plain_looped_ms_per_step": 1e3 * tp / steps,
-            "persistent_grid": [grid, thr], "mode": "persistent" if mode == 0 else "staged"}
+            "persistent_grid": [grid, thr],
+            "mode": ("autotuned " if chosen else "") + ("persistent" if (chosen[0] if chosen else mode) == 0 else "staged"),
+            "autotune_ms_per_step": chosen[2] if chosen else None}
 
 
 def _job_set(n_jobs: int, horizon_scale: float, seed: int):

@@ -384,6 +384,57 @@ SPH_API sph_status sph_batch_finalize(sph_batch* b)
     return SPH_OK;
 }
 
+// Autotuner: times `trial_steps` steps of the staged graph and of the
+// persistent kernel at 1..max CTAs per SM, on a saved copy of the state
+// (restored after every trial), and keeps the fastest configuration.
+SPH_API sph_status sph_batch_autotune(sph_batch* b, uint32_t trial_steps, int* mode_out, uint32_t* grid_out,
+                                      float* ms_per_step_out)
+{
+    if (!b || trial_steps == 0) return SPH_ERR_INVALID_ARGUMENT;
+    if (!b->finalized) API_TRY(sph_batch_finalize(b));
+    API_CUDA_TRY(cudaSetDevice(b->device));
+    StepState& st = b->state;
+    uint32_t sms = 0, per_sm = 0;
+    API_TRY(st.persistent_capacity(&sms, &per_sm));
+    API_TRY(st.save_state());
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    API_CUDA_TRY(cudaEventCreate(&e0));
+    API_CUDA_TRY(cudaEventCreate(&e1));
+    struct Trial { StepMode mode; uint32_t ctas; float ms; };
+    std::vector<Trial> trials;
+    trials.push_back({StepMode::Staged, 0, 0.f});
+    for (uint32_t c = 1; c <= per_sm; ++c) trials.push_back({StepMode::Persistent, c * sms, 0.f});
+    sph_status result = SPH_OK;
+    for (auto& t : trials) {
+        st.set_persistent_ctas(t.ctas);
+        // one untimed step (graph capture, first-launch costs), then timed steps
+        if ((result = st.enqueue_steps(1, t.mode, false, false)) != SPH_OK) break;
+        if (cudaEventRecord(e0, b->stream) != cudaSuccess) { result = SPH_ERR_CUDA; break; }
+        if ((result = st.enqueue_steps(trial_steps, t.mode, false, false)) != SPH_OK) break;
+        if (cudaEventRecord(e1, b->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) { result = SPH_ERR_CUDA; break; }
+        cudaEventElapsedTime(&t.ms, e0, e1);
+        t.ms /= (float)trial_steps;
+        if ((result = st.check_device_error()) != SPH_OK) break;
+        if ((result = st.restore_state()) != SPH_OK) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (result != SPH_OK) {
+        st.restore_state();
+        return result;
+    }
+    const Trial* best = &trials[0];
+    for (const auto& t : trials)
+        if (t.ms < best->ms) best = &t;
+    b->mode = best->mode;
+    st.set_persistent_ctas(best->ctas);
+    API_TRY(st.persistent_grid(&b->grid));
+    if (mode_out) *mode_out = best->mode == StepMode::Persistent ? 0 : 1;
+    if (grid_out) *grid_out = best->mode == StepMode::Persistent ? best->ctas : 0;
+    if (ms_per_step_out) *ms_per_step_out = best->ms;
+    return SPH_OK;
+}
+
 SPH_API sph_status sph_batch_set_mode(sph_batch* b, int mode)
 {
     if (!b || (mode != 0 && mode != 1)) return SPH_ERR_INVALID_ARGUMENT;

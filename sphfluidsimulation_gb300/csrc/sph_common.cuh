@@ -111,6 +111,7 @@ struct SceneDesc {
     uint32_t sq_off, t;
     uint32_t t_off, pad0;
     uint32_t sf_off, sf_buckets;   // neighbour-pass static table (power of two >= 8 s)
+    uint32_t sbm_off, sbm_mask;    // static-presence bitmap: word offset, bit-index mask
     FastMod fm_b;
     FastMod fm_s;
     FastMod fm_sf;
@@ -142,6 +143,19 @@ inline uint32_t fast_static_buckets(uint32_t s)
     uint64_t b = 1;
     while (b < want) b <<= 1;
     return (uint32_t)std::min<uint64_t>(b, 1ull << 30);
+}
+
+// Bits of a scene's static-presence bitmap: a power of two of about 64 bits
+// per static particle (at least 2^12, at most 2^27).  Bit (code & mask) is set
+// for every cell within one cell of a static particle, so a particle whose
+// own cell's bit is clear has no static neighbour within h.
+inline uint32_t static_bitmap_bits(uint32_t s)
+{
+    if (!s) return 0;
+    const uint64_t want = std::min<uint64_t>(std::max<uint64_t>(4096, 64ull * s), 1ull << 27);
+    uint64_t b = 1;
+    while (b < want) b <<= 1;
+    return (uint32_t)b;
 }
 
 // Smoothing kernel constant and self density (SF:115-125 as used by

@@ -58,6 +58,7 @@ struct StepArgs {
     const float4* spos;         // static particles sorted for the neighbour passes
     const uint32_t* sstart;     // their bucket table (global scan, power-of-two buckets)
     const float* tris;          // 9 floats per triangle
+    const uint32_t* sbitmap;    // static-presence bitmaps of all scenes
     float4* accel;              // optional: acceleration per sorted slot (.w unused)
     uint32_t* err;              // device status word
     uint32_t* bar_count;        // grid barrier (persistent kernel only)
@@ -533,7 +534,7 @@ __device__ __forceinline__ void density_homes(uint32_t tile_index, const SceneDe
                                               const float4 (&hp)[NH], const float4* __restrict__ pos,
                                               float4* __restrict__ vel, const uint32_t* __restrict__ start,
                                               const float4* __restrict__ spos, const uint32_t* __restrict__ sstart,
-                                              const NbrArgs& nl)
+                                              const uint32_t* __restrict__ sbitmap, const NbrArgs& nl)
 {
     const float h = sc.h, h2 = sc.h2;
     const float cull2 = __fmul_rn(h2, 1.0001f);
@@ -550,6 +551,9 @@ __device__ __forceinline__ void density_homes(uint32_t tile_index, const SceneDe
     const uint32_t span = nb_span(nb);
     const bool cull_d = box_ok && span < sc.buckets;
     const bool dup_s = span >= sc.s;     // reference static buckets may repeat
+    // no static particle within one cell: skip the 27 static bucket lookups
+    const uint32_t own = (nb.ex1 + nb.ey1 + nb.ez1) & sc.sbm_mask;
+    const bool near_static = sc.s && ((__ldg(sbitmap + sc.sbm_off + (own >> 5)) >> (own & 31u)) & 1u);
     const uint32_t delta = sc.p_off - __ldg(start + sc.q_off);
     const uint32_t sdelta = sc.s ? sc.s_off - __ldg(sstart + sc.sf_off) : 0u;
     const uint32_t stride = nl.stride;
@@ -586,7 +590,7 @@ __device__ __forceinline__ void density_homes(uint32_t tile_index, const SceneDe
                         }
                     }
                 }
-                if (sc.s && !(far && box_ok)) {
+                if (near_static && !(far && box_ok)) {
                     const uint32_t sb = sc.sf_off + fast_mod(hsh, sc.fm_sf);
                     const uint32_t sbeg = max(__ldg(sstart + sb) + sdelta, sc.s_off);
                     const uint32_t send = min(__ldg(sstart + sb + 1) + sdelta, sc.s_off + sc.s);
@@ -689,14 +693,30 @@ __device__ __forceinline__ void density_tile(uint32_t tile_index, const Tile& ti
                                              const SceneDesc* scenes, const float4* __restrict__ pos,
                                              float4* __restrict__ vel, const uint32_t* __restrict__ start,
                                              const float4* __restrict__ spos, const uint32_t* __restrict__ sstart,
-                                             const NbrArgs& nl)
+                                             const uint32_t* __restrict__ sbitmap, const NbrArgs& nl)
 {
     const SceneDesc& sc = scenes[tile.scene];
     const uint32_t i = tile.begin + lane;
     if (i >= tile.end) return;
     const uint32_t hi[1] = {i};
     const float4 hp[1] = {pos[i]};
-    density_homes<1>(tile_index, sc, hi, hp, pos, vel, start, spos, sstart, nl);
+    density_homes<1>(tile_index, sc, hi, hp, pos, vel, start, spos, sstart, sbitmap, nl);
+}
+
+// Marks, for every static particle, the bitmap bits of the 27 cells whose
+// neighbourhood holds its cell.
+__device__ __forceinline__ void static_bitmap_tile(const Tile& tile, const SceneDesc* scenes, const float4* spos,
+                                                   uint32_t* sbitmap)
+{
+    const SceneDesc& sc = scenes[tile.scene];
+    const uint32_t i = tile.begin + threadIdx.x;
+    if (i >= tile.end) return;
+    const float4 q = spos[i];
+    const Neighbourhood nb = neighbourhood(q.x, q.y, q.z, sc.h);
+    for (int k = 0; k < 27; ++k) {
+        const uint32_t code = neighbour_hash(nb, k / 9, (k / 3) % 3, k % 3) & sc.sbm_mask;
+        atomicOr(sbitmap + sc.sbm_off + (code >> 5), 1u << (code & 31u));
+    }
 }
 
 // ---- stage: force + integrate + rehash -------------------------------------

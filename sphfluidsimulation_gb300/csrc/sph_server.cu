@@ -114,7 +114,7 @@ struct Job {
     std::vector<float> pos, spos;
     uint32_t steps = 0, done = 0;
     JobState state = JobState::Queued;
-    uint64_t p_off = 0, q_off = 0, s_off = 0, sq_off = 0, sf_off = 0;
+    uint64_t p_off = 0, q_off = 0, s_off = 0, sq_off = 0, sf_off = 0, sb_off = 0;
     uint64_t bytes = 0;
     std::vector<sph_dynamic_particle> result;
     float gas = 1.f, rho0 = 0.f;
@@ -135,7 +135,8 @@ uint64_t job_bytes(uint32_t n, uint32_t s)
     // (96 + 48 slots) 576, list counts 4;
     // per static particle: two sorted copies 32, staging 32, bucket count +
     // start for both tables 8 + 8 x 8 = 72
-    return 704ull * n + 136ull * s + 4096ull;
+    // plus 8 bytes per static particle of static-presence bitmap
+    return 704ull * n + 144ull * s + 4096ull;
 }
 
 struct sph_server {
@@ -145,13 +146,14 @@ struct sph_server {
     uint32_t max_slots = 0;
     StepState arena;
     bool arena_ready = false;
-    RangeAlloc pa, qa, sa, sqa, sfa;
+    RangeAlloc pa, qa, sa, sqa, sfa, sba;
     uint64_t used_bytes = 0;
     uint64_t next_id = 1;
     std::unordered_map<uint64_t, std::unique_ptr<Job>> jobs;
     std::deque<uint64_t> queue;
     std::vector<uint64_t> active;
     bool dirty = false;
+    sph::StepMode mode = sph::StepMode::Staged;
 };
 
 #define SRV_CUDA_TRY(expr)                                                                     \
@@ -174,32 +176,36 @@ static sph_status ensure_room(sph_server* sv, const Job& j)
 {
     const uint64_t n = j.in.n, s = j.in.s, q = 2ull * j.in.n + 1, sq = (uint64_t)j.in.s + 1;
     const uint64_t sf = (uint64_t)sph::fast_static_buckets(j.in.s) + 1;
+    const uint64_t sb = sph::static_bitmap_bits(j.in.s) / 32 + 1;
     uint64_t need_n = sv->pa.needed_for(n), need_q = sv->qa.needed_for(q);
     uint64_t need_s = sv->sa.needed_for(s), need_sq = sv->sqa.needed_for(sq), need_sf = sv->sfa.needed_for(sf);
+    uint64_t need_sb = sv->sba.needed_for(sb);
     if (need_n <= sv->pa.cap() && need_q <= sv->qa.cap() && need_s <= sv->sa.cap() && need_sq <= sv->sqa.cap() &&
-        need_sf <= sv->sfa.cap())
+        need_sf <= sv->sfa.cap() && need_sb <= sv->sba.cap())
         return SPH_OK;
     auto grown = [](uint64_t need, uint64_t cap) { return need <= cap ? cap : std::max(need, cap * 2); };
     uint64_t cn = grown(need_n, sv->pa.cap()), cq = grown(need_q, sv->qa.cap());
     uint64_t cs = grown(need_s, sv->sa.cap()), csq = grown(need_sq, sv->sqa.cap());
-    uint64_t csf = grown(need_sf, sv->sfa.cap());
+    uint64_t csf = grown(need_sf, sv->sfa.cap()), csb = grown(need_sb, sv->sba.cap());
     const uint64_t limit = (1ull << 31) - 64;
-    if (cn > limit || cq > limit || cs > limit || csq > limit || csf > limit) {
+    if (cn > limit || cq > limit || cs > limit || csq > limit || csf > limit || csb > limit) {
         sph::set_last_error("arena index space exhausted");
         return SPH_ERR_CAPACITY;
     }
     if (!sv->arena_ready) {
         SRV_TRY(sv->arena.init_arena(sv->device, sv->stream, (uint32_t)cn, (uint32_t)cq, (uint32_t)cs, (uint32_t)csq,
-                                     (uint32_t)csf, sv->max_slots));
+                                     (uint32_t)csf, (uint32_t)csb, sv->max_slots));
         sv->arena_ready = true;
     } else {
-        SRV_TRY(sv->arena.grow_arena((uint32_t)cn, (uint32_t)cq, (uint32_t)cs, (uint32_t)csq, (uint32_t)csf));
+        SRV_TRY(sv->arena.grow_arena((uint32_t)cn, (uint32_t)cq, (uint32_t)cs, (uint32_t)csq, (uint32_t)csf,
+                                     (uint32_t)csb));
     }
     sv->pa.grow(cn);
     sv->qa.grow(cq);
     sv->sa.grow(cs);
     sv->sqa.grow(csq);
     sv->sfa.grow(csf);
+    sv->sba.grow(csb);
     return SPH_OK;
 }
 
@@ -211,6 +217,7 @@ static SceneDesc desc_of(const Job& j)
     d.s_off = (uint32_t)j.s_off;
     d.sq_off = (uint32_t)j.sq_off;
     d.sf_off = (uint32_t)j.sf_off;
+    d.sbm_off = (uint32_t)j.sb_off;
     return d;
 }
 
@@ -224,6 +231,7 @@ static sph_status admit(sph_server* sv, Job& j)
     ok = ok && sv->sa.alloc(s, &j.s_off);
     ok = ok && sv->sqa.alloc(sq, &j.sq_off);
     ok = ok && sv->sfa.alloc(sf, &j.sf_off);
+    ok = ok && sv->sba.alloc(sph::static_bitmap_bits(j.in.s) / 32 + 1, &j.sb_off);
     if (!ok) {
         sph::set_last_error("arena allocation failed after growth");
         return SPH_ERR_CAPACITY;
@@ -231,7 +239,7 @@ static sph_status admit(sph_server* sv, Job& j)
     SceneInput in = j.in;
     in.pos = j.pos.data();
     in.spos = j.spos.empty() ? nullptr : j.spos.data();
-    SRV_TRY(sv->arena.admit_scene(desc_of(j), in));
+    SRV_TRY(sv->arena.admit_scene(desc_of(j), in, /*sync=*/false));
     j.pos.clear();
     j.pos.shrink_to_fit();
     j.spos.clear();
@@ -250,6 +258,7 @@ static void release_ranges(sph_server* sv, Job& j)
     sv->sa.release(j.s_off, j.in.s);
     sv->sqa.release(j.sq_off, (uint64_t)j.in.s + 1);
     sv->sfa.release(j.sf_off, (uint64_t)sph::fast_static_buckets(j.in.s) + 1);
+    sv->sba.release(j.sb_off, sph::static_bitmap_bits(j.in.s) / 32 + 1);
     sv->used_bytes -= j.bytes;
 }
 
@@ -346,6 +355,7 @@ SPH_API sph_status sph_server_poll(sph_server* sv, uint32_t chunk_steps, uint32_
         }
     }
     if (!sv->active.empty()) {
+        SRV_TRY(sv->arena.check_device_error());   // the admissions' sorts
         if (sv->dirty) {
             std::vector<SceneDesc> descs;
             for (uint64_t id : sv->active) descs.push_back(desc_of(*sv->jobs[id]));
@@ -357,7 +367,7 @@ SPH_API sph_status sph_server_poll(sph_server* sv, uint32_t chunk_steps, uint32_
             const Job& j = *sv->jobs[id];
             steps = std::min(steps, j.steps - j.done);
         }
-        SRV_TRY(sv->arena.enqueue_steps(steps, sph::StepMode::Persistent, false, false));
+        SRV_TRY(sv->arena.enqueue_steps(steps, sv->mode, false, false));
         SRV_CUDA_TRY(cudaStreamSynchronize(sv->stream));
         SRV_TRY(sv->arena.check_device_error());
         std::vector<uint64_t> still;

@@ -79,11 +79,13 @@ public:
     // ---- arena mode (server): fixed-capacity arrays, each scene occupies
     // ranges of the slot / bucket / static index spaces chosen by the caller.
     sph_status init_arena(int device, cudaStream_t stream, uint32_t cap_n, uint32_t cap_q, uint32_t cap_s,
-                          uint32_t cap_sq, uint32_t cap_sf, uint32_t max_scenes);
+                          uint32_t cap_sq, uint32_t cap_sf, uint32_t cap_sbm, uint32_t max_scenes);
     // Grows every array to at least the given capacities, keeping contents.
-    sph_status grow_arena(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s, uint32_t cap_sq, uint32_t cap_sf);
+    sph_status grow_arena(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s, uint32_t cap_sq, uint32_t cap_sf,
+                          uint32_t cap_sbm);
     // Uploads one scene into its ranges (d's offsets) and sorts it alone.
-    sph_status admit_scene(const SceneDesc& d, const SceneInput& in);
+    // With sync = false the work is only queued (check_device_error later).
+    sph_status admit_scene(const SceneDesc& d, const SceneInput& in, bool sync = true);
     // Replaces the set of scenes the step advances (table, tiles, scan range).
     sph_status set_active(const std::vector<SceneDesc>& descs);
     uint32_t cap_n() const { return cap_n_; }
@@ -91,9 +93,21 @@ public:
     uint32_t cap_s() const { return cap_s_; }
     uint32_t cap_sq() const { return cap_sq_; }
     uint32_t cap_sf() const { return cap_sf_; }
+    uint32_t cap_sbm() const { return cap_sbm_; }
+
+    // Copies the state a step reads (sorted particles and the bucket table)
+    // aside and back, so trial steps leave the simulation where it was.
+    sph_status save_state();
+    sph_status restore_state();
+    // Occupancy-limited CTAs per SM of the persistent step kernel.
+    sph_status persistent_capacity(uint32_t* sms, uint32_t* per_sm);
 
     const float* stage_ms() const { return stage_ms_; }
-    void set_persistent_ctas(uint32_t c) { persistent_ctas_ = c; }
+    void set_persistent_ctas(uint32_t c)
+    {
+        persistent_ctas_ = c;
+        grid_cache_ = 0;
+    }
 
     std::vector<SceneDesc> scenes;
     std::vector<Tile> tiles, stiles;
@@ -119,6 +133,7 @@ public:
     uint32_t* snbr = nullptr;      // [kMaxSNbr][cap_n]
     uint32_t* ncount = nullptr;
     uint32_t* tile_overflow = nullptr;
+    uint32_t* sbitmap = nullptr;   // static-presence bitmaps (words)
     SceneDesc* d_sfscenes = nullptr;
     float* tris = nullptr;
     float4* accel = nullptr;
@@ -132,7 +147,7 @@ private:
     sph_status enqueue_sort(int kind);
     sph_status enqueue_scan(uint32_t* cnt, uint32_t* out, uint32_t len);
     sph_status alloc_arrays(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s, uint32_t cap_sq, uint32_t cap_sf,
-                            uint32_t cap_t, uint32_t max_scenes, uint32_t max_tiles);
+                            uint32_t cap_sbm, uint32_t cap_t, uint32_t max_scenes, uint32_t max_tiles);
     sph_status enqueue_step_staged(bool record_accel, bool timed);
     sph_status enqueue_step_persistent();
     sph_status ensure_events();
@@ -145,9 +160,14 @@ private:
     cudaEvent_t events_[6] = {};
     float stage_ms_[5] = {};
     uint32_t persistent_ctas_ = 0;
-    uint32_t cap_n_ = 0, cap_q_ = 0, cap_s_ = 0, cap_sq_ = 0, cap_sf_ = 0, cap_t_ = 0, max_scenes_ = 0, max_tiles_ = 0;
+    uint32_t grid_cache_ = 0;
+    uint32_t cap_n_ = 0, cap_q_ = 0, cap_s_ = 0, cap_sq_ = 0, cap_sf_ = 0, cap_sbm_ = 0, cap_t_ = 0, max_scenes_ = 0,
+             max_tiles_ = 0;
     std::vector<uint32_t> tile_first_;     // first tile of each scene
     Tile* d_tmp_tiles_ = nullptr;          // tiles of a scene being admitted
+    float4* saved_pos_ = nullptr;          // save_state() copies
+    float4* saved_vel_ = nullptr;
+    uint32_t* saved_start_ = nullptr;
     SceneDesc* d_tmp_scene_ = nullptr;     // its dynamic and two static views
 };
 

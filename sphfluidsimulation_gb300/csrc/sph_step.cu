@@ -54,7 +54,7 @@ __device__ __forceinline__ NbrArgs nbr_args(const StepArgs& a)
 __global__ void __launch_bounds__(kDensityThreads, SPH_DENSITY_MIN_CTAS) k_density(StepArgs a)
 {
     density_tile(blockIdx.x, a.tiles[blockIdx.x], threadIdx.x, a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart,
-                 nbr_args(a));
+                 a.sbitmap, nbr_args(a));
 }
 
 template <bool kRecord>
@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(kTileThreads) k_step_persistent(StepArgs a, ui
         a.scan_status[t] = 0ull;
     const NbrArgs nl = nbr_args(a);
     for (uint32_t t = blockIdx.x; t < a.num_tiles; t += gridDim.x)
-        density_tile(t, a.tiles[t], threadIdx.x, a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart, nl);
+        density_tile(t, a.tiles[t], threadIdx.x, a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart, a.sbitmap, nl);
     grid_barrier(a.bar_count, a.bar_gen, a.err);
     for (uint32_t t = blockIdx.x; t < a.num_tiles; t += gridDim.x) {
         force_tile<false>(a.tiles[t], a.scenes, a.pos, a.vel, a.spos, a.tris, nl, a.pos_tmp, a.vel_tmp, a.key,
@@ -136,6 +136,12 @@ __global__ void __launch_bounds__(kTileThreads) k_step_persistent(StepArgs a, ui
     for (uint32_t t = blockIdx.x; t < a.num_tiles; t += gridDim.x)
         gather_tile(a.tiles[t], a.scenes, a.key, a.arrival, a.perm, a.start, a.pos_tmp, a.vel_tmp, a.pos, a.vel,
                     a.err);
+}
+
+__global__ void __launch_bounds__(kTileThreads) k_static_bitmap(const Tile* tiles, const SceneDesc* scenes,
+                                                                const float4* spos, uint32_t* sbitmap)
+{
+    static_bitmap_tile(tiles[blockIdx.x], scenes, spos, sbitmap);
 }
 
 // Readback: sorted slot i -> caller's order, in the reference's 32-byte layout
@@ -212,12 +218,16 @@ void StepState::release()
     if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
     void* ptrs[] = {d_scenes, d_sscenes, d_sfscenes, d_tiles, d_stiles, pos, vel, pos_tmp, vel_tmp, key, arrival,
                     perm, count, start, scan_status, scan_ticket, err, bar, spos, sstart, spos_ref, sstart_ref, tris,
-                    accel, accel_io, staging, d_tmp_tiles_, d_tmp_scene_, nbr, snbr, ncount, tile_overflow};
+                    accel, accel_io, staging, d_tmp_tiles_, d_tmp_scene_, nbr, snbr, ncount, tile_overflow,
+                    saved_pos_, saved_vel_, saved_start_, sbitmap};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     d_scenes = d_sscenes = d_sfscenes = d_tmp_scene_ = nullptr;
+    saved_pos_ = saved_vel_ = nullptr;
+    saved_start_ = nullptr;
+    grid_cache_ = 0;
     spos_ref = nullptr;
-    sstart_ref = nbr = snbr = ncount = tile_overflow = nullptr;
+    sstart_ref = nbr = snbr = ncount = tile_overflow = sbitmap = nullptr;
     d_tiles = d_stiles = d_tmp_tiles_ = nullptr;
     pos = vel = pos_tmp = vel_tmp = spos = accel = accel_io = nullptr;
     staging = nullptr;
@@ -233,7 +243,7 @@ void StepState::release()
     tile_first_.clear();
     total_n = total_s = total_t = 0;
     scan_len = sscan_len = sfscan_len = 0;
-    cap_n_ = cap_q_ = cap_s_ = cap_sq_ = cap_sf_ = cap_t_ = max_scenes_ = max_tiles_ = 0;
+    cap_n_ = cap_q_ = cap_s_ = cap_sq_ = cap_sf_ = cap_sbm_ = cap_t_ = max_scenes_ = max_tiles_ = 0;
 }
 
 static SceneDesc make_scene_desc(const sph_params& p, float dt)
@@ -265,6 +275,7 @@ SceneDesc scene_desc_for(const SceneInput& in)
     d.fm_s = make_fastmod(in.s);
     d.sf_buckets = fast_static_buckets(in.s);
     d.fm_sf = make_fastmod(d.sf_buckets);
+    d.sbm_mask = in.s ? static_bitmap_bits(in.s) - 1u : 0u;
     return d;
 }
 
@@ -307,8 +318,9 @@ static uint32_t tiles_for(uint32_t n) { return (n + kTileThreads - 1) / kTileThr
 // Allocates every device array for the given capacities (all zero-filled
 // where the algorithm needs zeros: bucket counters, scan status, errors).
 sph_status StepState::alloc_arrays(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s, uint32_t cap_sq, uint32_t cap_sf,
-                                   uint32_t cap_t, uint32_t max_scenes, uint32_t max_tiles)
+                                   uint32_t cap_sbm, uint32_t cap_t, uint32_t max_scenes, uint32_t max_tiles)
 {
+    cap_sbm_ = cap_sbm;
     cap_n_ = cap_n;
     cap_q_ = cap_q;
     cap_s_ = cap_s;
@@ -350,6 +362,7 @@ sph_status StepState::alloc_arrays(uint32_t cap_n, uint32_t cap_q, uint32_t cap_
     ALLOC(snbr, (size_t)kMaxSNbr * cap_n);
     ALLOC(ncount, cap_n);
     ALLOC(tile_overflow, max_tiles_);
+    ALLOC(sbitmap, cap_sbm);
     ALLOC(tris, 9ull * cap_t);
     ALLOC(staging, 2ull * work_n);
 #undef ALLOC
@@ -358,6 +371,7 @@ sph_status StepState::alloc_arrays(uint32_t cap_n, uint32_t cap_q, uint32_t cap_
     CUDA_TRY(cudaMemsetAsync(bar, 0, 2 * sizeof(uint32_t), stream_));
     CUDA_TRY(cudaMemsetAsync(scan_status, 0, sizeof(unsigned long long) * scan_tiles_max, stream_));
     CUDA_TRY(cudaMemsetAsync(tile_overflow, 0, sizeof(uint32_t) * max_tiles_, stream_));
+    CUDA_TRY(cudaMemsetAsync(sbitmap, 0, sizeof(uint32_t) * std::max<uint32_t>(cap_sbm, 1), stream_));
     CUDA_TRY(cudaStreamSynchronize(stream_));
     return SPH_OK;
 }
@@ -378,8 +392,9 @@ static sph_status upload_particles(cudaStream_t stream, float4* staging, uint32_
             hbuf[8ull * i + 6] = v[3ull * i + 2];
         }
     }
+    // from pageable memory the call returns once the data is staged, so the
+    // host buffer may be released right away; stream order does the rest
     CUDA_TRY(cudaMemcpyAsync(staging + 2ull * off, hbuf.data(), sizeof(float) * hbuf.size(), cudaMemcpyHostToDevice, stream));
-    CUDA_TRY(cudaStreamSynchronize(stream));
     return SPH_OK;
 }
 
@@ -388,7 +403,7 @@ sph_status StepState::build(int device, cudaStream_t stream, const std::vector<S
     release();
     device_ = device;
     stream_ = stream;
-    uint64_t p_off = 0, q_off = 0, s_off = 0, sq_off = 0, sf_off = 0, t_off = 0;
+    uint64_t p_off = 0, q_off = 0, s_off = 0, sq_off = 0, sf_off = 0, sbm_off = 0, t_off = 0;
     for (size_t k = 0; k < inputs.size(); ++k) {
         const SceneInput& in = inputs[k];
         sph_status st = validate_scene(in);
@@ -399,6 +414,7 @@ sph_status StepState::build(int device, cudaStream_t stream, const std::vector<S
         d.s_off = (uint32_t)s_off;
         d.sq_off = (uint32_t)sq_off;
         d.sf_off = (uint32_t)sf_off;
+        d.sbm_off = (uint32_t)sbm_off;
         d.t_off = (uint32_t)t_off;
         scenes.push_back(d);
         tile_first_.push_back((uint32_t)tiles.size());
@@ -411,6 +427,7 @@ sph_status StepState::build(int device, cudaStream_t stream, const std::vector<S
         s_off += in.s;
         sq_off += in.s;
         sf_off += d.sf_buckets;
+        sbm_off += in.s ? (d.sbm_mask + 1ull) / 32 : 0;
         t_off += in.t;
         if (p_off > kMaxParticles || s_off > kMaxParticles || q_off >= (1ull << 31) || sf_off >= (1ull << 31)) {
             set_last_error("total particle or bucket count exceeds the 32-bit index space");
@@ -423,8 +440,9 @@ sph_status StepState::build(int device, cudaStream_t stream, const std::vector<S
     scan_len = (uint32_t)q_off + 1u;
     sscan_len = (uint32_t)sq_off + 1u;
     sfscan_len = (uint32_t)sf_off + 1u;
-    sph_status st = alloc_arrays(total_n, (uint32_t)q_off, total_s, (uint32_t)sq_off, (uint32_t)sf_off, total_t,
-                                 (uint32_t)scenes.size(), (uint32_t)std::max(tiles.size(), stiles.size()));
+    sph_status st = alloc_arrays(total_n, (uint32_t)q_off, total_s, (uint32_t)sq_off, (uint32_t)sf_off,
+                                 (uint32_t)sbm_off, total_t, (uint32_t)scenes.size(),
+                                 (uint32_t)std::max(tiles.size(), stiles.size()));
     if (st != SPH_OK) return st;
     std::vector<SceneDesc> sview, sfview;
     for (const auto& d : scenes) {
@@ -452,6 +470,8 @@ sph_status StepState::build(int device, cudaStream_t stream, const std::vector<S
         if ((st = enqueue_load(staging, /*statics=*/true)) != SPH_OK) return st;
         if ((st = enqueue_sort(1)) != SPH_OK) return st;
         if ((st = enqueue_sort(2)) != SPH_OK) return st;
+        k_static_bitmap<<<(unsigned)stiles.size(), kTileThreads, 0, stream_>>>(d_stiles, d_scenes, spos, sbitmap);
+        CUDA_TRY(cudaGetLastError());
         CUDA_TRY(cudaStreamSynchronize(stream_));
     }
     for (size_t k = 0; k < inputs.size(); ++k)
@@ -468,12 +488,12 @@ sph_status StepState::build(int device, cudaStream_t stream, const std::vector<S
 // ---- arena mode ---------------------------------------------------------------
 
 sph_status StepState::init_arena(int device, cudaStream_t stream, uint32_t cap_n, uint32_t cap_q, uint32_t cap_s,
-                                 uint32_t cap_sq, uint32_t cap_sf, uint32_t max_scenes)
+                                 uint32_t cap_sq, uint32_t cap_sf, uint32_t cap_sbm, uint32_t max_scenes)
 {
     release();
     device_ = device;
     stream_ = stream;
-    return alloc_arrays(cap_n, cap_q, cap_s, cap_sq, cap_sf, 0, max_scenes, tiles_for(cap_n) + max_scenes);
+    return alloc_arrays(cap_n, cap_q, cap_s, cap_sq, cap_sf, cap_sbm, 0, max_scenes, tiles_for(cap_n) + max_scenes);
 }
 
 template <typename T>
@@ -492,14 +512,18 @@ static sph_status grow_one(T** p, size_t old_count, size_t new_count, bool zero_
     return SPH_OK;
 }
 
-sph_status StepState::grow_arena(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s, uint32_t cap_sq, uint32_t cap_sf)
+sph_status StepState::grow_arena(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s, uint32_t cap_sq, uint32_t cap_sf,
+                                 uint32_t cap_sbm)
 {
     cap_n = std::max(cap_n, cap_n_);
     cap_q = std::max(cap_q, cap_q_);
     cap_s = std::max(cap_s, cap_s_);
     cap_sq = std::max(cap_sq, cap_sq_);
     cap_sf = std::max(cap_sf, cap_sf_);
-    if (cap_n == cap_n_ && cap_q == cap_q_ && cap_s == cap_s_ && cap_sq == cap_sq_ && cap_sf == cap_sf_) return SPH_OK;
+    cap_sbm = std::max(cap_sbm, cap_sbm_);
+    if (cap_n == cap_n_ && cap_q == cap_q_ && cap_s == cap_s_ && cap_sq == cap_sq_ && cap_sf == cap_sf_ &&
+        cap_sbm == cap_sbm_)
+        return SPH_OK;
     if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
     const size_t old_work = std::max(cap_n_, cap_s_), new_work = std::max(cap_n, cap_s);
     const size_t old_cnt = std::max(std::max(cap_q_, cap_sq_), cap_sf_) + 1ull;
@@ -525,6 +549,7 @@ sph_status StepState::grow_arena(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s,
     GROW(snbr, 0, (size_t)kMaxSNbr * cap_n, false);
     GROW(ncount, 0, cap_n, false);
     GROW(tile_overflow, 0, tiles_for(cap_n) + max_scenes_, true);
+    GROW(sbitmap, cap_sbm_, std::max<uint32_t>(cap_sbm, 1), true);
     GROW(scan_status, 0, new_scan_tiles, true);
     GROW(d_tmp_tiles_, 0, tiles_for((uint32_t)new_work) + 1, false);
     GROW(d_tiles, 0, tiles_for(cap_n) + max_scenes_, false);
@@ -538,17 +563,18 @@ sph_status StepState::grow_arena(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s,
     cap_s_ = cap_s;
     cap_sq_ = cap_sq;
     cap_sf_ = cap_sf;
+    cap_sbm_ = cap_sbm;
     return set_active(scenes);
 }
 
 // Sorts one scene alone: its own tiles and one-entry scene tables, and scans
 // over its own bucket ranges only, so every other scene's table is untouched
 // (a sub-range scan yields local starts; the per-scene delta absorbs that).
-sph_status StepState::admit_scene(const SceneDesc& d, const SceneInput& in)
+sph_status StepState::admit_scene(const SceneDesc& d, const SceneInput& in, bool sync)
 {
     if (d.p_off + (uint64_t)d.n > cap_n_ || d.q_off + (uint64_t)d.buckets > cap_q_ ||
         d.s_off + (uint64_t)d.s > cap_s_ || d.sq_off + (uint64_t)d.s > cap_sq_ ||
-        d.sf_off + (uint64_t)d.sf_buckets > cap_sf_) {
+        d.sf_off + (uint64_t)d.sf_buckets > cap_sf_ || (d.s && d.sbm_off + (d.sbm_mask + 1ull) / 32 > cap_sbm_)) {
         set_last_error("scene ranges exceed the arena");
         return SPH_ERR_CAPACITY;
     }
@@ -590,9 +616,13 @@ sph_status StepState::admit_scene(const SceneDesc& d, const SceneInput& in)
         CUDA_TRY(cudaGetLastError());
         k_gather<<<nt, kTileThreads, 0, stream_>>>(a);
         CUDA_TRY(cudaGetLastError());
-        CUDA_TRY(cudaStreamSynchronize(stream_));
+        if (kind == 2) {   // this scene's static-presence bitmap, from its sorted statics
+            CUDA_TRY(cudaMemsetAsync(sbitmap + d.sbm_off, 0, sizeof(uint32_t) * ((d.sbm_mask + 1ull) / 32), stream_));
+            k_static_bitmap<<<nt, kTileThreads, 0, stream_>>>(d_tmp_tiles_, d_tmp_scene_, spos, sbitmap);
+            CUDA_TRY(cudaGetLastError());
+        }
     }
-    return check_device_error();
+    return sync ? check_device_error() : SPH_OK;
 }
 
 sph_status StepState::set_active(const std::vector<SceneDesc>& descs)
@@ -710,6 +740,7 @@ StepArgs StepState::step_args() const
     a.spos = spos;
     a.sstart = sstart;
     a.tris = tris;
+    a.sbitmap = sbitmap;
     a.accel = accel;
     a.err = err;
     a.bar_count = bar;
@@ -764,6 +795,10 @@ sph_status StepState::enqueue_step_staged(bool record_accel, bool timed)
 
 sph_status StepState::persistent_grid(uint32_t* grid)
 {
+    if (grid_cache_) {
+        *grid = grid_cache_;
+        return SPH_OK;
+    }
     int sms = 0, per_sm = 0;
     CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step_persistent, kTileThreads, 0));
@@ -771,6 +806,7 @@ sph_status StepState::persistent_grid(uint32_t* grid)
     uint32_t g = (uint32_t)(sms * per_sm);
     if (persistent_ctas_ && persistent_ctas_ < g) g = persistent_ctas_;
     *grid = std::max<uint32_t>(1, g);
+    grid_cache_ = *grid;
     return SPH_OK;
 }
 
@@ -980,6 +1016,39 @@ sph_status StepState::read_sort(uint32_t* keys, uint32_t* counts, uint32_t* star
         for (uint32_t i = 0; i < d.n; ++i) std::memcpy(&order[i], &tmp[i].w, 4);
     }
     return check_device_error();
+}
+
+sph_status StepState::save_state()
+{
+    sph_status st;
+    if (!saved_pos_ && (st = dev_alloc(&saved_pos_, cap_n_)) != SPH_OK) return st;
+    if (!saved_vel_ && (st = dev_alloc(&saved_vel_, cap_n_)) != SPH_OK) return st;
+    if (!saved_start_ && (st = dev_alloc(&saved_start_, cap_q_ + 1ull)) != SPH_OK) return st;
+    CUDA_TRY(cudaMemcpyAsync(saved_pos_, pos, sizeof(float4) * cap_n_, cudaMemcpyDeviceToDevice, stream_));
+    CUDA_TRY(cudaMemcpyAsync(saved_vel_, vel, sizeof(float4) * cap_n_, cudaMemcpyDeviceToDevice, stream_));
+    CUDA_TRY(cudaMemcpyAsync(saved_start_, start, sizeof(uint32_t) * (cap_q_ + 1ull), cudaMemcpyDeviceToDevice, stream_));
+    CUDA_TRY(cudaStreamSynchronize(stream_));
+    return SPH_OK;
+}
+
+sph_status StepState::restore_state()
+{
+    if (!saved_pos_ || !saved_vel_ || !saved_start_) return SPH_ERR_NOT_INITIALIZED;
+    CUDA_TRY(cudaMemcpyAsync(pos, saved_pos_, sizeof(float4) * cap_n_, cudaMemcpyDeviceToDevice, stream_));
+    CUDA_TRY(cudaMemcpyAsync(vel, saved_vel_, sizeof(float4) * cap_n_, cudaMemcpyDeviceToDevice, stream_));
+    CUDA_TRY(cudaMemcpyAsync(start, saved_start_, sizeof(uint32_t) * (cap_q_ + 1ull), cudaMemcpyDeviceToDevice, stream_));
+    CUDA_TRY(cudaStreamSynchronize(stream_));
+    return SPH_OK;
+}
+
+sph_status StepState::persistent_capacity(uint32_t* sms, uint32_t* per_sm)
+{
+    int s = 0, b = 0;
+    CUDA_TRY(cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, device_));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_step_persistent, kTileThreads, 0));
+    *sms = (uint32_t)s;
+    *per_sm = (uint32_t)std::max(b, 1);
+    return SPH_OK;
 }
 
 }  // namespace sph

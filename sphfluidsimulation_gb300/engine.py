@@ -218,6 +218,15 @@ class Batch:
     def step(self, steps: int = 1) -> None:
         check(self.lib.sph_batch_step(self.h, int(steps)), "sph_batch_step")
 
+    def autotune(self, trial_steps: int = 3):
+        """(mode, grid_ctas, ms_per_step) of the configuration chosen."""
+        mode = C.c_int()
+        grid = C.c_uint32()
+        ms = C.c_float()
+        check(self.lib.sph_batch_autotune(self.h, int(trial_steps), C.byref(mode), C.byref(grid), C.byref(ms)),
+              "sph_batch_autotune")
+        return mode.value, grid.value, ms.value
+
     def read_scene(self, scene_id: int) -> np.ndarray:
         out = np.zeros(self.sizes[scene_id], DYN_DTYPE)
         check(self.lib.sph_batch_read_scene(self.h, int(scene_id), out.ctypes.data_as(C.c_void_p)),

@@ -68,3 +68,16 @@ def test_batch_info_and_empty_scene():
     assert tot == scs[0].n + scs[1].n
     assert grid >= 1 and thr == 128
     assert b.read_scene(eid).shape == (0,)
+
+
+def test_autotune_keeps_state_and_results():
+    scs = uneven_scenes()
+    b = Batch()
+    ids = [b.add_scene(sc) for sc in scs]
+    b.finalize()
+    mode, grid, ms = b.autotune(2)
+    assert mode in (0, 1) and ms > 0
+    assert (grid > 0) == (mode == 0)
+    b.step(12)
+    for sid, sc in zip(ids, scs):
+        assert b.read_scene(sid).tobytes() == alone(sc, 12).tobytes(), sc.name
