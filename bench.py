@@ -150,17 +150,23 @@ def max_over_ranks(pg, value: float, local: int) -> float:
 # CPU baseline (the oracle port of the reference CPU engine, threaded)
 # ---------------------------------------------------------------------------
 
-def cpu_baseline(scene, steps: int, warmup: int, threads: int):
+def cpu_baseline(scene, target_s: float, max_steps: int, threads: int):
+    """The oracle port of the reference CPU engine on `threads` host threads:
+    one timed warm-up step sizes the sample to about `target_s` seconds of
+    CPU work (at most `max_steps` steps), then one update() call over those
+    steps is timed.  Returns (particle-steps/s, seconds, steps)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_lib import Oracle
     o = Oracle(threads)
     o.init(scene)
-    if warmup:
-        o.update(scene.dt, warmup)
+    t0 = time.perf_counter()
+    o.update(scene.dt, 1)
+    per_step = max(time.perf_counter() - t0, 1e-6)
+    steps = max(1, min(max_steps, int(target_s / per_step)))
     t0 = time.perf_counter()
     o.update(scene.dt, steps)
     dt = time.perf_counter() - t0
-    return scene.n * steps / dt, dt
+    return scene.n * steps / dt, dt, steps
 
 
 def run_reference(args):
@@ -169,12 +175,11 @@ def run_reference(args):
         return 0
     threads = os.cpu_count() or 1
     scene = workload_scene(args.workload if args.workload not in ("batched", "served") else "dam_break_1m", 1)
-    # bounded sample: the steps of this run, capped so the run stays within minutes
-    per_step_s = scene.n / 3.0e6
-    steps = max(1, min(args.steps, int(60.0 / max(per_step_s, 1e-3))))
-    warm = min(args.warmup, 1)
-    value, secs = cpu_baseline(scene, steps, warm, threads)
-    sample = f"{scene.name}: {scene.n} particles, {steps} timed steps after {warm} warm-up, one Update() call"
+    # bounded sample: the steps of this run, capped at about a minute of CPU work
+    warm = 1
+    value, secs, steps = cpu_baseline(scene, 60.0, args.steps, threads)
+    sample = (f"{scene.name}: {scene.n} particles, {steps} timed steps after {warm} warm-up, "
+              f"one update() call ({secs:.1f} s)")
     line = {
         "impl": "reference", "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
         "n_gpus": world, "steps": steps, "warmup": warm, "ms_per_step": 1000.0 * secs / steps,
@@ -279,7 +284,9 @@ def run_plain(args, world, rank, local, pg):
                      "alg_bytes_per_launch": alg_bytes(dom_name, n, s)},
         "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": 32 * n,
                 "d2h_bytes_per_step": 32 * n, "steps": e2e_steps},
-        "gpu_launches": 5 * args.steps,
+        # per step: density, force, overflow force, scan, scatter, gather
+        # (the scan's two memsets are not kernels)
+        "gpu_launches": 6 * args.steps,
         "clocks": clk,
         "wall_s_timed_region": wall,
     }
@@ -312,6 +319,8 @@ def main():
     ap.add_argument("--workload", default="dam_break_1m",
                     choices=["dam_break_1m", "dam_break_16k", "pool_drop_8m", "batched", "served"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the bounded batched/served samples in the default line")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -327,12 +336,21 @@ def main():
         scene = None
     else:
         line, scene = run_plain(args, world, rank, local, pg)
+    if rank == 0 and scene is not None and not args.no_forms and world == 1:
+        # bounded samples of the two production forms on the same GPU
+        from sphfluidsimulation_gb300 import bench_forms
+        b = bench_forms.run_batched(min(args.steps, 20))
+        line["batched"] = {k: b[k] for k in ("scenes", "particles", "steps", "batched_particle_steps_per_s",
+                                             "plain_looped_particle_steps_per_s", "speedup", "mode")}
+        sv = bench_forms.run_served(n_jobs=64, horizon_scale=0.05)
+        line["served"] = {k: sv[k] for k in ("jobs", "horizon_scale", "served_particle_steps_per_s",
+                                             "fifo_plain_particle_steps_per_s", "speedup", "served_latency",
+                                             "fifo_latency", "load_vs_fifo_capacity")}
+        line["served"]["sample"] = "64 jobs of the 2,000-job mix, horizons x0.05; full run: --workload served"
     if rank == 0:
         if scene is not None and not args.no_cpu_baseline and world == 1:
             threads = os.cpu_count() or 1
-            per_step_s = scene.n / 3.0e6
-            steps = max(1, min(5, int(20.0 / max(per_step_s, 1e-3))))
-            v, secs = cpu_baseline(scene, steps, 1, threads)
+            v, secs, steps = cpu_baseline(scene, 15.0, 1000, threads)
             line["cpu_baseline"] = {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": "port",
                                     "sample": f"{scene.name}: {scene.n} particles, {steps} steps after 1 warm-up "
                                               f"({secs:.1f} s), oracle port of the reference CPU engine"}
