@@ -95,8 +95,12 @@ SPH_API sph_status sph_engine_clear(sph_engine* engine);
  *   dyn_vel     n x 3 floats or NULL (the reference starts at rest)
  *   static_pos  s x 3 floats, the "static" layer positions (may be NULL if s=0)
  *   triangles   t x 9 floats, boundary mesh triangles (may be NULL if t=0)
- *   reorder_time_interval  the scene's "reorderTimeInterval" (accepted; this
- *               engine keeps particles physically sorted every step)
+ *   reorder_time_interval  the scene's "reorderTimeInterval"
+ *               (SimulationEngineCPU.cpp:401; FLT_MAX = never reorder).  The
+ *               engine keeps particles sorted by bucket in memory every step;
+ *               the interval decides, as in the reference, when a particle's
+ *               buffer index is renumbered, and that index orders the members
+ *               of a bucket in the neighbour passes
  * Bucket count is 2n (SimulationEngineCPU.cpp:486), static buckets s. */
 SPH_API sph_status sph_engine_initialize(sph_engine* engine, const sph_params* params,
                                          const float* dyn_pos, const float* dyn_vel, uint32_t n,
@@ -122,6 +126,12 @@ SPH_API sph_status sph_engine_synchronize(sph_engine* engine);
  * the caller's input order (out has n entries). */
 SPH_API sph_status sph_engine_read_dynamic(sph_engine* engine, sph_dynamic_particle* out);
 
+/* The same particles in the reference's own buffer order: out[k] is the
+ * particle at index k of SimulationEngineCPU's current buffer (the initial
+ * bucket sort, SimulationEngineCPU.cpp:69-128, then renumbered by every
+ * reordering step, SF:332-345), i.e. the bytes LockRead() returns there. */
+SPH_API sph_status sph_engine_read_dynamic_buffer(sph_engine* engine, sph_dynamic_particle* out);
+
 /* LockWrite()-style upload: replaces every particle's position and velocity
  * (input order; pressure and hash are ignored) and re-sorts. */
 SPH_API sph_status sph_engine_write_dynamic(sph_engine* engine, const sph_dynamic_particle* in);
@@ -146,6 +156,16 @@ SPH_API const char* sph_engine_implementation_name(void);
 /* Particle counts: which = 0 dynamic, 1 static, 2 dynamic buckets, 3 triangles. */
 SPH_API sph_status sph_engine_count(sph_engine* engine, int which, uint64_t* value);
 
+/* Arithmetic of the neighbour passes.  exact = 0 (the default): fused
+ * multiply-adds and reciprocal multiplies; results agree with the reference
+ * to rounding (density to about 3e-7 relative).  exact = 1: the reference's
+ * own operations one for one (SPHFunctions.cpp:358-656 with IEEE Vec3
+ * operators), in the reference's visiting order, so every step reproduces
+ * the bits of SimulationEngineCPU run synchronously; the one exception is a
+ * pair of particles at the same position, whose RandomDirection uses the
+ * sine of the platform's math library.  The exact form costs some speed. */
+SPH_API sph_status sph_engine_set_exact(sph_engine* engine, int exact);
+
 /* Debug output: when on, each step also stores the acceleration
  * F/rho + g of every particle; read it (input order, n x 3) after a step. */
 SPH_API sph_status sph_engine_record_acceleration(sph_engine* engine, int on);
@@ -162,14 +182,15 @@ SPH_API sph_status sph_engine_kernel_times(sph_engine* engine, float* ms, int co
 SPH_API sph_status sph_engine_get_stream(sph_engine* engine, void** stream);
 
 /* ---- the counting sort stage on its own ---------------------------------
- * Hash + count + scan + stable scatter of n positions into `buckets` buckets
- * with cell size h, on the device (SF:321-356 with the serial scan of
+ * Hash + count + scan + scatter of n positions into `buckets` buckets with
+ * cell size h, on the device (SF:321-356 with the serial scan of
  * SimulationEngineCPU.cpp:245-253).  Outputs (each may be NULL):
  *   keys    n     key of each input position, GetHash(GetCell(p)) % buckets
  *   counts  buckets  particles per bucket
  *   starts  buckets+1  bucket start slots, starts[buckets] = n
- *   order   n     input index of the particle in each slot (stable: ties keep
- *                 input order) */
+ *   order   n     input index of the particle in each slot; inside a bucket
+ *                 by decreasing input index, the slots the reference's fill
+ *                 gives (SF:346-356: slot = --count[key] over i = 0..n-1) */
 SPH_API sph_status sph_cell_sort(int device, const float* pos, uint32_t n, float h, uint32_t buckets,
                                  uint32_t* keys, uint32_t* counts, uint32_t* starts, uint32_t* order);
 

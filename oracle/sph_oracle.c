@@ -232,6 +232,9 @@ typedef struct sph_oracle {
     _Atomic uint32_t* hash_map;  /* B+1 entries, hash_map[B] = N (ECPU:486-487) */
     uint32_t* particle_map;      /* N entries */
     uint32_t* init_order;        /* slot -> input index after the init sort */
+    uint32_t* ident;             /* slot of the current buffer -> input index (bookkeeping only:
+                                    the reference keeps no identity; reorders permute it) */
+    uint32_t* ident_tmp;
 
     static_particle* statics;    /* bucket-sorted static particles */
     uint32_t* static_map;        /* S+1 entries (ECPU:468) */
@@ -461,7 +464,10 @@ static void simulate_steps(sph_oracle* o, uint32_t tid, uint32_t nthreads, real 
                 uint32_t slot = atomic_fetch_sub_explicit(&o->hash_map[out[i].hash], 1u, memory_order_relaxed) - 1u;
                 o->particle_map[i] = i;
                 ordered[slot] = out[i];
+                o->ident_tmp[slot] = o->ident[i];
             }
+            sync_threads(o, nthreads);
+            if (tid == 0) { uint32_t* t = o->ident; o->ident = o->ident_tmp; o->ident_tmp = t; }
         } else {                                                                   /* SF:346-356 */
             for (uint32_t i = begin; i < end; ++i) {
                 uint32_t slot = atomic_fetch_sub_explicit(&o->hash_map[out[i].hash], 1u, memory_order_relaxed) - 1u;
@@ -498,6 +504,8 @@ static void release(sph_oracle* o)
     free(o->hash_map); o->hash_map = NULL;
     free(o->particle_map); o->particle_map = NULL;
     free(o->init_order); o->init_order = NULL;
+    free(o->ident); o->ident = NULL;
+    free(o->ident_tmp); o->ident_tmp = NULL;
     free(o->statics); o->statics = NULL;
     free(o->static_map); o->static_map = NULL;
     free(o->triangles); o->triangles = NULL;
@@ -558,6 +566,8 @@ static void init_dynamic(sph_oracle* o, const float* pos, const float* vel, uint
     atomic_store(&o->hash_map[B], N);
     o->particle_map = (uint32_t*)calloc(N, sizeof(uint32_t));
     o->init_order = (uint32_t*)calloc(N, sizeof(uint32_t));
+    o->ident = (uint32_t*)calloc(N, sizeof(uint32_t));
+    o->ident_tmp = (uint32_t*)calloc(N, sizeof(uint32_t));
     for (int k = 0; k < 3; ++k) o->buffers[k] = (dyn_particle*)calloc(N, sizeof(dyn_particle));
 
     dyn_particle* initial = o->buffers[0];
@@ -586,6 +596,7 @@ static void init_dynamic(sph_oracle* o, const float* pos, const float* vel, uint
         o->particle_map[i] = i;
         final_[slot] = initial[i];
         o->init_order[slot] = i;
+        o->ident[slot] = i;
     }
     o->current = 1;
 }
@@ -708,7 +719,7 @@ EXPORT void sph_oracle_read_maps(const sph_oracle* o, uint32_t* hash_map, uint32
 {
     if (hash_map) for (uint32_t k = 0; k <= o->buckets && o->n; ++k) hash_map[k] = atomic_load(&o->hash_map[k]);
     if (particle_map) memcpy(particle_map, o->particle_map, sizeof(uint32_t) * (size_t)o->n);
-    if (init_order) memcpy(init_order, o->init_order, sizeof(uint32_t) * (size_t)o->n);
+    if (init_order) memcpy(init_order, o->ident, sizeof(uint32_t) * (size_t)o->n);
 }
 
 EXPORT void sph_oracle_read_static(const sph_oracle* o, double* pos4, uint32_t* static_map)

@@ -53,12 +53,14 @@ _SIGS = {
     "sph_engine_update_async": (_st, [_vp, C.c_float, C.c_uint32]),
     "sph_engine_synchronize": (_st, [_vp]),
     "sph_engine_read_dynamic": (_st, [_vp, _vp]),
+    "sph_engine_read_dynamic_buffer": (_st, [_vp, _vp]),
     "sph_engine_write_dynamic": (_st, [_vp, _vp]),
     "sph_engine_read_static": (_st, [_vp, _vp, _up]),
     "sph_engine_read_buckets": (_st, [_vp, _up, _up]),
     "sph_engine_simulation_time": (_st, [_vp, _dp]),
     "sph_engine_count": (_st, [_vp, C.c_int, _u64p]),
     "sph_engine_record_acceleration": (_st, [_vp, C.c_int]),
+    "sph_engine_set_exact": (_st, [_vp, C.c_int]),
     "sph_engine_read_acceleration": (_st, [_vp, _fp]),
     "sph_engine_set_timing": (_st, [_vp, C.c_int]),
     "sph_engine_kernel_times": (_st, [_vp, _fp, C.c_int]),

@@ -22,7 +22,8 @@ struct sph_engine {
     StepState state;
     bool initialized = false;
     double sim_time = 0.0;
-    float reorder_interval = 0.f;
+    float reorder_interval = 0.f;   // "reorderTimeInterval" (SimulationEngineCPU.cpp:401)
+    float reorder_elapsed = 0.f;    // reorderParticlesElapsedTime
     bool record_accel = false;
     bool timing = false;
     bool accel_valid = false;
@@ -125,6 +126,7 @@ SPH_API sph_status sph_engine_clear(sph_engine* e)
     e->state.release();
     e->initialized = false;
     e->sim_time = 0.0;
+    e->reorder_elapsed = 0.f;
     e->n = e->s = e->t = 0;
     e->accel_valid = false;
     return SPH_OK;
@@ -162,10 +164,15 @@ static sph_status engine_enqueue(sph_engine* e, float dt, uint32_t steps)
         sph::set_last_error("Update called on an uninitialized engine");
         return SPH_ERR_NOT_INITIALIZED;
     }
-    if (e->n == 0 || steps == 0) return SPH_OK;
+    if (e->n == 0) return SPH_OK;
     API_CUDA_TRY(cudaSetDevice(e->device));
+    // SimulationEngineCPU.cpp:441,452-454: one reorder decision per call, for
+    // all of its steps; the elapsed time advances by dt per call
+    API_TRY(e->state.set_reorder(0, e->reorder_elapsed > e->reorder_interval));
     API_TRY(e->state.set_dt(0, dt));
     API_TRY(e->state.enqueue_steps(steps, StepMode::Staged, e->record_accel, e->timing));
+    e->reorder_elapsed += dt;
+    if (e->reorder_elapsed > e->reorder_interval) e->reorder_elapsed = 0.f;
     e->sim_time += (double)dt * steps;
     e->accel_valid = e->record_accel;
     return SPH_OK;
@@ -196,6 +203,14 @@ SPH_API sph_status sph_engine_read_dynamic(sph_engine* e, sph_dynamic_particle* 
     if (!e->initialized) return SPH_ERR_NOT_INITIALIZED;
     API_CUDA_TRY(cudaSetDevice(e->device));
     return e->state.read_scene(0, out, nullptr);
+}
+
+SPH_API sph_status sph_engine_read_dynamic_buffer(sph_engine* e, sph_dynamic_particle* out)
+{
+    if (!e || (!out && e->n)) return SPH_ERR_INVALID_ARGUMENT;
+    if (!e->initialized) return SPH_ERR_NOT_INITIALIZED;
+    API_CUDA_TRY(cudaSetDevice(e->device));
+    return e->state.read_scene(0, out, nullptr, /*buffer_order=*/true);
 }
 
 SPH_API sph_status sph_engine_write_dynamic(sph_engine* e, const sph_dynamic_particle* in)
@@ -239,6 +254,15 @@ SPH_API sph_status sph_engine_count(sph_engine* e, int which, uint64_t* value)
     case 3: *value = e->t; break;
     default: return SPH_ERR_INVALID_ARGUMENT;
     }
+    return SPH_OK;
+}
+
+SPH_API sph_status sph_engine_set_exact(sph_engine* e, int exact)
+{
+    if (!e) return SPH_ERR_INVALID_ARGUMENT;
+    API_CUDA_TRY(cudaSetDevice(e->device));
+    API_CUDA_TRY(cudaStreamSynchronize(e->stream));
+    e->state.set_exact(exact != 0);
     return SPH_OK;
 }
 

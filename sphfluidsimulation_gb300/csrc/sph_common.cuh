@@ -109,7 +109,8 @@ struct SceneDesc {
     uint32_t q_off, buckets;
     uint32_t s_off, s;
     uint32_t sq_off, t;
-    uint32_t t_off, pad0;
+    uint32_t t_off;
+    uint32_t reorder;              // 1: this step's sort renumbers buffer tags (SimulationEngineCPU.cpp:290-303)
     uint32_t sf_off, sf_buckets;   // neighbour-pass static table (power of two >= 8 s)
     uint32_t sbm_off, sbm_mask;    // static-presence bitmap: word offset, bit-index mask
     FastMod fm_b;

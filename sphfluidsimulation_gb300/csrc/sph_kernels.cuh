@@ -7,13 +7,19 @@
 //   hash_count_tile      SF:321-331  key + warp-aggregated bucket count
 //   scan_tile            SF:227-294  single-pass decoupled-lookback scan
 //   scatter_tile         SF:346-356  slot = bucket start + arrival rank
-//   gather_tile          SF:332-345  stable rank inside the bucket + SoA move
+//   gather_tile          SF:332-345  rank inside the bucket by buffer tag + SoA move
 //   density_tile         SF:358-501  27-bucket density / pressure pass
 //   force_tile           SF:503-656  27-bucket force, integrate, rehash
 //
 // Data layout (struct of arrays, sorted by bucket every step):
 //   pos[i] = (x, y, z, input index as bits)
 //   vel[i] = (vx, vy, vz, pressure)       pressure written by the density pass
+//   tag[i] = the particle's index in the reference's particle buffer
+//
+// The neighbour passes come in two arithmetic forms.  kExact = false (the
+// default) fuses multiply-adds and divides by a reciprocal; kExact = true
+// repeats the reference's operations one for one, so with the same visiting
+// order its results are the reference's bits.
 #pragma once
 #include "sph_common.cuh"
 
@@ -49,7 +55,8 @@ struct StepArgs {
     float4* vel_tmp;
     uint32_t* key;              // local bucket of the new position, per tmp slot
     uint32_t* arrival;          // arrival rank inside the bucket, per tmp slot
-    uint32_t* perm;             // slot -> tmp slot (arrival order)
+    uint32_t* ptag;             // scatter slot -> buffer tag of the particle placed there
+    uint32_t* tag;              // buffer tag per sorted slot (the reference's buffer index)
     uint32_t* count;            // bucket counters, zero between steps
     uint32_t* start;            // exclusive scan of count
     uint32_t scan_len;          // entries of count/start scanned
@@ -57,6 +64,8 @@ struct StepArgs {
     uint32_t* scan_ticket;
     const float4* spos;         // static particles sorted for the neighbour passes
     const uint32_t* sstart;     // their bucket table (global scan, power-of-two buckets)
+    const float4* spos_ref;     // static particles in the reference's own s-bucket order
+    const uint32_t* sstart_ref; // its bucket table
     const float* tris;          // 9 floats per triangle
     const uint32_t* sbitmap;    // static-presence bitmaps of all scenes
     float4* accel;              // optional: acceleration per sorted slot (.w unused)
@@ -359,10 +368,21 @@ __device__ inline void scan_tile(uint32_t tile, uint32_t* count, uint32_t* start
 }
 
 // ---- stage: scatter (arrival order) ----------------------------------------
+//
+// Every particle lands on slot start + arrival rank and leaves its buffer tag
+// there: tag_src[j] when the sort carries tags, else the source slot j.
+
+// What the gather writes to tag_dst.
+enum TagAssign : uint32_t {
+    kTagNone = 0,    // no tags (static sorts)
+    kTagSlot = 1,    // the new slot inside the scene (the initial sort)
+    kTagKeep = 2,    // the source tag (a write between steps)
+    kTagStep = 3,    // per scene: the new slot on a reordering step, else the source tag
+};
 
 __device__ __forceinline__ void scatter_tile(const Tile& tile, const SceneDesc* scenes, const uint32_t* key,
-                                             const uint32_t* arrival, const uint32_t* start, uint32_t* perm,
-                                             uint32_t* err)
+                                             const uint32_t* arrival, const uint32_t* start,
+                                             const uint32_t* tag_src, uint32_t* ptag, uint32_t* err)
 {
     const SceneDesc& sc = scenes[tile.scene];
     const uint32_t i = tile.begin + threadIdx.x;
@@ -370,21 +390,27 @@ __device__ __forceinline__ void scatter_tile(const Tile& tile, const SceneDesc* 
     const uint32_t delta = sc.p_off - start[sc.q_off];
     const uint32_t slot = start[sc.q_off + key[i]] + delta + arrival[i];
     if (slot - sc.p_off >= sc.n) { set_error(err, DEV_ERR_SLOT_RANGE); return; }
-    perm[slot] = i;
+    ptag[slot] = tag_src ? tag_src[i] : i;
 }
 
 // ---- stage: stable gather --------------------------------------------------
 //
-// Source slot j moves to bucket start + (number of the bucket's members with
-// a smaller source slot), so each bucket keeps the previous slot order: a
-// deterministic, stable counting sort.  Buckets hold a handful of particles,
-// so the rank loop reads a few words from L1.
+// Inside a bucket the members are ordered by decreasing tag: source slot j
+// moves to bucket start + (number of members with a larger tag).  That is
+// the order every counting sort of the reference produces, which fills each
+// bucket from its end while it walks the buffer upwards
+// (SimulationEngine.h:96-97, SF:332-356 with SimulationEngineCPU.cpp:288-316),
+// so the neighbour passes visit a bucket's members exactly as the reference
+// does.  Tags are the reference's buffer indices: fixed between reorders,
+// renumbered to the new slot by a reordering step.  Buckets hold a handful
+// of particles, so the rank loop reads a few words from L1.
 constexpr uint32_t kStableRankLimit = 8192;   // larger buckets keep arrival order
 
 __device__ __forceinline__ void gather_tile(const Tile& tile, const SceneDesc* scenes, const uint32_t* key,
-                                            const uint32_t* arrival, const uint32_t* perm, const uint32_t* start,
+                                            const uint32_t* arrival, const uint32_t* ptag, const uint32_t* start,
                                             const float4* pos_src, const float4* vel_src, float4* pos_dst,
-                                            float4* vel_dst, uint32_t* err)
+                                            float4* vel_dst, uint32_t* tag_dst, uint32_t assign, uint32_t* err,
+                                            const float4* accel_src = nullptr, float4* accel_dst = nullptr)
 {
     const SceneDesc& sc = scenes[tile.scene];
     const uint32_t j = tile.begin + threadIdx.x;
@@ -394,9 +420,12 @@ __device__ __forceinline__ void gather_tile(const Tile& tile, const SceneDesc* s
     const uint32_t b0 = start[g] + delta;
     const uint32_t e0 = start[g + 1] + delta;
     if (b0 - sc.p_off > sc.n || e0 - sc.p_off > sc.n || e0 < b0) { set_error(err, DEV_ERR_BUCKET_RANGE); return; }
+    const uint32_t mine_at = b0 + arrival[j];
+    if (mine_at >= e0) { set_error(err, DEV_ERR_SLOT_RANGE); return; }
+    const uint32_t mine = ptag[mine_at];
     uint32_t rank = 0;
     if (e0 - b0 <= kStableRankLimit) {
-        for (uint32_t t = b0; t < e0; ++t) rank += (perm[t] < j) ? 1u : 0u;
+        for (uint32_t t = b0; t < e0; ++t) rank += (ptag[t] > mine) ? 1u : 0u;
     } else {
         rank = arrival[j];
     }
@@ -404,6 +433,11 @@ __device__ __forceinline__ void gather_tile(const Tile& tile, const SceneDesc* s
     if (dst >= e0) { set_error(err, DEV_ERR_SLOT_RANGE); return; }
     pos_dst[dst] = pos_src[j];
     vel_dst[dst] = vel_src[j];
+    if (accel_src) accel_dst[dst] = accel_src[j];
+    if (assign != kTagNone) {
+        const bool renumber = assign == kTagSlot || (assign == kTagStep && sc.reorder);
+        tag_dst[dst] = renumber ? dst - sc.p_off : mine;
+    }
 }
 
 // Squared distance with a fixed rounding sequence, so every kernel that
@@ -484,25 +518,6 @@ __device__ __forceinline__ uint32_t nb_span(const Neighbourhood& nb)
     return span3(nb.ex0, nb.ex1, nb.ex2) + span3(nb.ey0, nb.ey1, nb.ey2) + span3(nb.ez0, nb.ez1, nb.ez2);
 }
 
-// How many of the 27 neighbour cells share cell k's bucket in the reference's
-// s-bucket static table (hash % s): the reference walks that bucket once per
-// such cell, so each static neighbour in cell k counts that many times
-// (SF:452-490 with SimulationEngineCPU.cpp:468).  1 unless the neighbourhood's
-// Morton codes span at least s.
-__device__ __noinline__ inline uint32_t static_multiplicity(const Neighbourhood& nb, const FastMod& fm_s, uint32_t hk)
-{
-    const uint32_t target = fast_mod(hk, fm_s);
-    uint32_t m = 0;
-    for (int a = 0; a < 3; ++a)
-        for (int b = 0; b < 3; ++b)
-            for (int c = 0; c < 3; ++c)
-                m += fast_mod(neighbour_hash(nb, a, b, c), fm_s) == target ? 1u : 0u;
-    return m;
-}
-
-constexpr uint32_t kMultShift = 27;                    // static list entry: index | multiplicity << 27
-constexpr uint32_t kIndexMask = (1u << kMultShift) - 1u;
-
 __device__ __forceinline__ float w0_of(float r2, float h)
 {
     const float r = __fsqrt_rn(r2);
@@ -510,197 +525,192 @@ __device__ __forceinline__ float w0_of(float r2, float h)
     return r < h ? __fmul_rn(__fmul_rn(w, w), w) : 0.f;
 }
 
-// Squared distances from q to the NH home particles, bit-identical to dist2().
-template <int NH>
-struct HomeCoords {
-    float4 p[NH];
-};
-
-template <int NH>
-__device__ __forceinline__ void dist2_n(const float4& q, const HomeCoords<NH>& hc, float (&r2)[NH])
+// Squared distance in the reference's own arithmetic: dir = q - p, then
+// dot(dir, dir) summed left to right with no contraction (SF:437-438 and the
+// Vec3 dot product).  dist2() above fuses the two adds; both round each step.
+__device__ __forceinline__ float dist2_ref(const float4& q, const float4& p)
 {
-#pragma unroll
-    for (int k = 0; k < NH; ++k) r2[k] = dist2(q, hc.p[k]);
+    const float dx = __fsub_rn(q.x, p.x), dy = __fsub_rn(q.y, p.y), dz = __fsub_rn(q.z, p.z);
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
 }
 
-// The density pass for NH home particles of one cell.  Every candidate is
-// loaded once for all homes; each home gets its own list, sums, counts and
-// pressure, identical to what it would get alone.  The step uses NH = 1: on
-// GB300 two homes per thread (with packed FP32x2 arithmetic) measured 3x
-// slower, the extra registers costing more occupancy than the shared loads
-// saved.
-template <int NH>
-__device__ __forceinline__ void density_homes(uint32_t tile_index, const SceneDesc& sc, const uint32_t (&hi)[NH],
-                                              const float4 (&hp)[NH], const float4* __restrict__ pos,
-                                              float4* __restrict__ vel, const uint32_t* __restrict__ start,
-                                              const float4* __restrict__ spos, const uint32_t* __restrict__ sstart,
-                                              const uint32_t* __restrict__ sbitmap, const NbrArgs& nl)
+template <bool kExact>
+__device__ __forceinline__ float pair_r2(const float4& q, const float4& p)
 {
-    const float h = sc.h, h2 = sc.h2;
+    return kExact ? dist2_ref(q, p) : dist2(q, p);
+}
+
+// Static neighbour list entries: an index into the neighbour-pass table, or,
+// with bit 31 set, into the reference's own s-bucket table.  Particles whose
+// 27 static buckets may repeat walk that table itself, visiting every bucket
+// as the reference does, so a static particle reached through two cells is
+// listed twice, in the reference's order.
+constexpr uint32_t kRefTableBit = 1u << 31;
+
+// The static tables the neighbour passes read.
+struct StaticTables {
+    const float4* spos;         // neighbour-pass table: sorted statics, w = cell Morton code
+    const uint32_t* sstart;
+    const float4* spos_ref;     // the reference's table (hash % s)
+    const uint32_t* sstart_ref;
+    const uint32_t* sbitmap;    // static-presence bitmaps
+};
+
+// What a neighbour walk of one particle needs to know about its 27 cells.
+struct Walk {
+    Neighbourhood nb;
+    CellBox box;
+    bool cull_d;        // dynamic buckets are distinct: cells beyond h may be skipped
+    bool dup_s;         // the reference's static buckets may repeat
+    bool near_static;   // a static particle lies within one cell
+    bool ref_walk;      // statics walk the reference's own table (dup_s)
+};
+
+template <bool kExact>
+__device__ __forceinline__ Walk make_walk(const SceneDesc& sc, const float4& p, const uint32_t* sbitmap)
+{
+    Walk w;
+    w.nb = neighbourhood(p.x, p.y, p.z, sc.h);
+    w.box = cell_box(p, sc.h);
+    const uint32_t span = nb_span(w.nb);
+    w.cull_d = w.box.ok && span < sc.buckets;
+    w.dup_s = span >= sc.s;
+    const uint32_t own = (w.nb.ex1 + w.nb.ey1 + w.nb.ez1) & sc.sbm_mask;
+    w.near_static = sc.s && ((__ldg(sbitmap + sc.sbm_off + (own >> 5)) >> (own & 31u)) & 1u);
+    w.ref_walk = w.near_static && w.dup_s;
+    return w;
+}
+
+// Visits the neighbours of slot i within h in the reference's order: the 27
+// cells x outermost (SF:392-395), each cell's dynamic bucket members in
+// bucket order (on_dyn(j, q, r2)), then its static ones (on_static(entry, q,
+// r2)).  Dynamic and static sums are separate in the reference, so only the
+// order inside each kind matters.  Cells whose box lies beyond h are skipped
+// when their bucket cannot hold another visited cell's particles.
+template <bool kExact, typename FD, typename FS>
+__device__ __forceinline__ void walk_neighbours(const SceneDesc& sc, uint32_t i, const float4& p, const Walk& w,
+                                                const float4* __restrict__ pos, const uint32_t* __restrict__ start,
+                                                const StaticTables& st, FD&& on_dyn, FS&& on_static)
+{
+    const float h2 = sc.h2;
     const float cull2 = __fmul_rn(h2, 1.0001f);
-    HomeCoords<NH> hc;
-    CellBox box[NH];
-    bool box_ok = true;
-#pragma unroll
-    for (int k = 0; k < NH; ++k) {
-        hc.p[k] = hp[k];
-        box[k] = cell_box(hp[k], h);
-        box_ok = box_ok && box[k].ok;
-    }
-    const Neighbourhood nb = neighbourhood(hp[0].x, hp[0].y, hp[0].z, h);
-    const uint32_t span = nb_span(nb);
-    const bool cull_d = box_ok && span < sc.buckets;
-    const bool dup_s = span >= sc.s;     // reference static buckets may repeat
-    // no static particle within one cell: skip the 27 static bucket lookups
-    const uint32_t own = (nb.ex1 + nb.ey1 + nb.ez1) & sc.sbm_mask;
-    const bool near_static = sc.s && ((__ldg(sbitmap + sc.sbm_off + (own >> 5)) >> (own & 31u)) & 1u);
     const uint32_t delta = sc.p_off - __ldg(start + sc.q_off);
-    const uint32_t sdelta = sc.s ? sc.s_off - __ldg(sstart + sc.sf_off) : 0u;
-    const uint32_t stride = nl.stride;
-    uint32_t cnt[NH], scnt[NH];
-#pragma unroll
-    for (int k = 0; k < NH; ++k) cnt[k] = scnt[k] = 0;
+    uint32_t sdelta = 0;
+    if (w.near_static)
+        sdelta = sc.s_off - (w.ref_walk ? __ldg(st.sstart_ref + sc.sq_off) : __ldg(st.sstart + sc.sf_off));
 #pragma unroll 1
     for (int a = 0; a < 3; ++a)
 #pragma unroll 1
         for (int b = 0; b < 3; ++b)
 #pragma unroll 1
             for (int c = 0; c < 3; ++c) {
-                bool far = true;
-#pragma unroll
-                for (int k = 0; k < NH; ++k) {
-                    const float bd2 = pick3f(a, box[k].x0, 0.f, box[k].x2) + pick3f(b, box[k].y0, 0.f, box[k].y2) +
-                                      pick3f(c, box[k].z0, 0.f, box[k].z2);
-                    far = far && bd2 > cull2;
-                }
-                const uint32_t hsh = neighbour_hash(nb, a, b, c);
-                if (!(far && cull_d)) {
+                const float bd2 = pick3f(a, w.box.x0, 0.f, w.box.x2) + pick3f(b, w.box.y0, 0.f, w.box.y2) +
+                                  pick3f(c, w.box.z0, 0.f, w.box.z2);
+                const bool far = bd2 > cull2;
+                const uint32_t hsh = neighbour_hash(w.nb, a, b, c);
+                if (!(far && w.cull_d)) {
                     const uint32_t bk = sc.q_off + fast_mod(hsh, sc.fm_b);
                     const uint32_t beg = max(__ldg(start + bk) + delta, sc.p_off);
                     const uint32_t end = min(__ldg(start + bk + 1) + delta, sc.p_off + sc.n);
                     for (uint32_t j = beg; j < end; ++j) {
-                        float r2[NH];
-                        dist2_n<NH>(__ldg(pos + j), hc, r2);
-#pragma unroll
-                        for (int k = 0; k < NH; ++k) {
-                            if (r2[k] <= h2 && j != hi[k]) {
-                                if (cnt[k] < kMaxNbr) nl.nbr[(size_t)cnt[k] * stride + hi[k]] = j;
-                                ++cnt[k];
-                            }
-                        }
+                        const float4 q = __ldg(pos + j);
+                        const float r2 = pair_r2<kExact>(q, p);
+                        if (r2 <= h2 && j != i) on_dyn(j, q, r2);
                     }
                 }
-                if (near_static && !(far && box_ok)) {
-                    const uint32_t sb = sc.sf_off + fast_mod(hsh, sc.fm_sf);
-                    const uint32_t sbeg = max(__ldg(sstart + sb) + sdelta, sc.s_off);
-                    const uint32_t send = min(__ldg(sstart + sb + 1) + sdelta, sc.s_off + sc.s);
-                    uint32_t mult = 0;
+                if (!w.near_static) continue;
+                if (w.ref_walk) {
+                    // SF:454-490: bucket hash % s of the reference's table, every member
+                    const uint32_t sb = sc.sq_off + fast_mod(hsh, sc.fm_s);
+                    const uint32_t sbeg = max(__ldg(st.sstart_ref + sb) + sdelta, sc.s_off);
+                    const uint32_t send = min(__ldg(st.sstart_ref + sb + 1) + sdelta, sc.s_off + sc.s);
                     for (uint32_t j = sbeg; j < send; ++j) {
-                        const float4 q = __ldg(spos + j);
+                        const float4 q = __ldg(st.spos_ref + j);
+                        const float r2 = pair_r2<kExact>(q, p);
+                        if (r2 <= h2) on_static(j | kRefTableBit, q, r2);
+                    }
+                } else if (!(far && w.box.ok)) {
+                    const uint32_t sb = sc.sf_off + fast_mod(hsh, sc.fm_sf);
+                    const uint32_t sbeg = max(__ldg(st.sstart + sb) + sdelta, sc.s_off);
+                    const uint32_t send = min(__ldg(st.sstart + sb + 1) + sdelta, sc.s_off + sc.s);
+                    for (uint32_t j = sbeg; j < send; ++j) {
+                        const float4 q = __ldg(st.spos + j);
                         // statics carry their cell's Morton code: only this cell's count
                         if (__float_as_uint(q.w) != hsh) continue;
-                        float r2[NH];
-                        dist2_n<NH>(q, hc, r2);
-#pragma unroll
-                        for (int k = 0; k < NH; ++k) {
-                            if (r2[k] <= h2) {
-                                if (!mult) mult = dup_s ? static_multiplicity(nb, sc.fm_s, hsh) : 1u;
-                                if (scnt[k] < kMaxSNbr)
-                                    nl.snbr[(size_t)scnt[k] * stride + hi[k]] = j | (mult << kMultShift);
-                                ++scnt[k];
-                            }
-                        }
+                        const float r2 = pair_r2<kExact>(q, p);
+                        if (r2 <= h2) on_static(j, q, r2);
                     }
                 }
             }
-#pragma unroll
-    for (int k = 0; k < NH; ++k) {
-        const uint32_t i = hi[k];
-        const float4 p = hp[k];
-        float sum_d = 0.f, sum_s = 0.f;
-        if (cnt[k] <= kMaxNbr) {
-            // four neighbours per round: their loads are issued together
-            const uint32_t* lp = nl.nbr + i;
-            uint32_t m = 0;
-            for (; SPH_NBR_BATCH == 4 && m + 4 <= cnt[k]; m += 4, lp += 4 * (size_t)stride) {
-                const uint32_t j0 = lp[0], j1 = lp[stride], j2 = lp[2 * (size_t)stride], j3 = lp[3 * (size_t)stride];
-                const float4 q0 = __ldg(pos + j0), q1 = __ldg(pos + j1), q2 = __ldg(pos + j2), q3 = __ldg(pos + j3);
-                sum_d = __fadd_rn(sum_d, w0_of(dist2(q0, p), h));
-                sum_d = __fadd_rn(sum_d, w0_of(dist2(q1, p), h));
-                sum_d = __fadd_rn(sum_d, w0_of(dist2(q2, p), h));
-                sum_d = __fadd_rn(sum_d, w0_of(dist2(q3, p), h));
-            }
-            for (; m < cnt[k]; ++m, lp += stride)
-                sum_d = __fadd_rn(sum_d, w0_of(dist2(__ldg(pos + *lp), p), h));
-        }
-        if (scnt[k] <= kMaxSNbr) {
-            const uint32_t* lp = nl.snbr + i;
-            for (uint32_t m = 0; m < scnt[k]; ++m, lp += stride) {
-                const uint32_t e = *lp;
-                const float w0 = w0_of(dist2(__ldg(spos + (e & kIndexMask)), p), h);
-                for (uint32_t r = e >> kMultShift; r; --r) sum_s = __fadd_rn(sum_s, w0);
-            }
-        }
-        if (cnt[k] > kMaxNbr || scnt[k] > kMaxSNbr) {
-            // overflow: walk the buckets again for this home, summing directly
-            const Neighbourhood nbk = neighbourhood(p.x, p.y, p.z, h);
-#pragma unroll 1
-            for (int a = 0; a < 3; ++a)
-#pragma unroll 1
-                for (int b = 0; b < 3; ++b)
-#pragma unroll 1
-                    for (int c = 0; c < 3; ++c) {
-                        const uint32_t hsh = neighbour_hash(nbk, a, b, c);
-                        if (cnt[k] > kMaxNbr) {
-                            const uint32_t bk = sc.q_off + fast_mod(hsh, sc.fm_b);
-                            const uint32_t beg = max(__ldg(start + bk) + delta, sc.p_off);
-                            const uint32_t end = min(__ldg(start + bk + 1) + delta, sc.p_off + sc.n);
-                            for (uint32_t j = beg; j < end; ++j) {
-                                const float r2 = dist2(__ldg(pos + j), p);
-                                if (r2 <= h2 && j != i) sum_d = __fadd_rn(sum_d, w0_of(r2, h));
-                            }
-                        }
-                        if (sc.s && scnt[k] > kMaxSNbr) {
-                            const uint32_t sb = sc.sf_off + fast_mod(hsh, sc.fm_sf);
-                            const uint32_t sbeg = max(__ldg(sstart + sb) + sdelta, sc.s_off);
-                            const uint32_t send = min(__ldg(sstart + sb + 1) + sdelta, sc.s_off + sc.s);
-                            uint32_t mult = 0;
-                            for (uint32_t j = sbeg; j < send; ++j) {
-                                const float4 q = __ldg(spos + j);
-                                const float r2 = dist2(q, p);
-                                if (__float_as_uint(q.w) == hsh && r2 <= h2) {
-                                    if (!mult) mult = dup_s ? static_multiplicity(nbk, sc.fm_s, hsh) : 1u;
-                                    const float w0 = w0_of(r2, h);
-                                    for (uint32_t r = mult; r; --r) sum_s = __fadd_rn(sum_s, w0);
-                                }
-                            }
-                        }
-                    }
-            atomicOr(nl.tile_overflow + tile_index, 1u);   // cleared by the overflow force pass
-        }
-        nl.ncount[i] = (cnt[k] > kMaxNbr ? kOverflow : cnt[k]) | ((scnt[k] > kMaxSNbr ? kOverflow : scnt[k]) << 16);
-        const float rho = __fadd_rn(sc.self_density,
-                                    __fmul_rn(__fadd_rn(__fmul_rn(sum_d, sc.mass), __fmul_rn(sum_s, sc.mass)), sc.kc));
-        const float pressure = __fmul_rn(sc.gas, __fsub_rn(rho, sc.rho0));
-        reinterpret_cast<float*>(vel + i)[3] = pressure;
-    }
+}
+
+// Position of a static list entry.
+__device__ __forceinline__ float4 static_entry_pos(uint32_t e, const StaticTables& st)
+{
+    return (e & kRefTableBit) ? __ldg(st.spos_ref + (e & ~kRefTableBit)) : __ldg(st.spos + e);
 }
 
 constexpr int kDensityThreads = kTileThreads;   // one home slot per thread
 
-// One tile of the density pass: thread `lane` owns slot tile.begin + lane.
+// One slot per thread.  (Two home particles per thread sharing candidate
+// loads measured 3x slower on GB300: the extra registers cost more occupancy
+// than the loads saved.)
+template <bool kExact>
 __device__ __forceinline__ void density_tile(uint32_t tile_index, const Tile& tile, uint32_t lane,
                                              const SceneDesc* scenes, const float4* __restrict__ pos,
                                              float4* __restrict__ vel, const uint32_t* __restrict__ start,
-                                             const float4* __restrict__ spos, const uint32_t* __restrict__ sstart,
-                                             const uint32_t* __restrict__ sbitmap, const NbrArgs& nl)
+                                             const StaticTables& st, const NbrArgs& nl)
 {
     const SceneDesc& sc = scenes[tile.scene];
     const uint32_t i = tile.begin + lane;
     if (i >= tile.end) return;
-    const uint32_t hi[1] = {i};
-    const float4 hp[1] = {pos[i]};
-    density_homes<1>(tile_index, sc, hi, hp, pos, vel, start, spos, sstart, sbitmap, nl);
+    const float h = sc.h;
+    const float4 p = pos[i];
+    const Walk w = make_walk<kExact>(sc, p, st.sbitmap);
+    const uint32_t stride = nl.stride;
+    uint32_t cnt = 0, scnt = 0;
+    walk_neighbours<kExact>(
+        sc, i, p, w, pos, start, st,
+        [&](uint32_t j, const float4&, float) {
+            if (cnt < kMaxNbr) nl.nbr[(size_t)cnt * stride + i] = j;
+            ++cnt;
+        },
+        [&](uint32_t e, const float4&, float) {
+            if (scnt < kMaxSNbr) nl.snbr[(size_t)scnt * stride + i] = e;
+            ++scnt;
+        });
+    float sum_d = 0.f, sum_s = 0.f;
+    const bool overflow = cnt > kMaxNbr || scnt > kMaxSNbr;
+    if (!overflow) {
+        // four neighbours per round: their loads are issued together
+        const uint32_t* lp = nl.nbr + i;
+        uint32_t m = 0;
+        for (; SPH_NBR_BATCH == 4 && m + 4 <= cnt; m += 4, lp += 4 * (size_t)stride) {
+            const uint32_t j0 = lp[0], j1 = lp[stride], j2 = lp[2 * (size_t)stride], j3 = lp[3 * (size_t)stride];
+            const float4 q0 = __ldg(pos + j0), q1 = __ldg(pos + j1), q2 = __ldg(pos + j2), q3 = __ldg(pos + j3);
+            sum_d = __fadd_rn(sum_d, w0_of(pair_r2<kExact>(q0, p), h));
+            sum_d = __fadd_rn(sum_d, w0_of(pair_r2<kExact>(q1, p), h));
+            sum_d = __fadd_rn(sum_d, w0_of(pair_r2<kExact>(q2, p), h));
+            sum_d = __fadd_rn(sum_d, w0_of(pair_r2<kExact>(q3, p), h));
+        }
+        for (; m < cnt; ++m, lp += stride) sum_d = __fadd_rn(sum_d, w0_of(pair_r2<kExact>(__ldg(pos + *lp), p), h));
+        lp = nl.snbr + i;
+        for (uint32_t k = 0; k < scnt; ++k, lp += stride)
+            sum_s = __fadd_rn(sum_s, w0_of(pair_r2<kExact>(static_entry_pos(*lp, st), p), h));
+    } else {
+        // overflow: walk the cells again, summing directly
+        walk_neighbours<kExact>(
+            sc, i, p, w, pos, start, st,
+            [&](uint32_t, const float4&, float r2) { sum_d = __fadd_rn(sum_d, w0_of(r2, h)); },
+            [&](uint32_t, const float4&, float r2) { sum_s = __fadd_rn(sum_s, w0_of(r2, h)); });
+        atomicOr(nl.tile_overflow + tile_index, 1u);   // cleared by the overflow force pass
+    }
+    nl.ncount[i] = overflow ? (kOverflow | (kOverflow << 16)) : (cnt | (scnt << 16));
+    // SF:497-498
+    const float rho = __fadd_rn(sc.self_density,
+                                __fmul_rn(__fadd_rn(__fmul_rn(sum_d, sc.mass), __fmul_rn(sum_s, sc.mass)), sc.kc));
+    const float pressure = __fmul_rn(sc.gas, __fsub_rn(rho, sc.rho0));
+    reinterpret_cast<float*>(vel + i)[3] = pressure;
 }
 
 // Marks, for every static particle, the bitmap bits of the 27 cells whose
@@ -735,16 +745,35 @@ struct PairSums {
     float3 fp, fv, fs;
 };
 
+// Coincident pair: the reference's RandomDirection((float)threadID), its
+// thread being the particle's buffer index (SF:576-580, 610-614).  The fast
+// form seeds with the input index instead, which keeps the tag array out of
+// the force loop's registers.
+template <bool kExact>
+__device__ __forceinline__ float3 coincident_direction(const float4& p, const uint32_t* tag, uint32_t i)
+{
+    return random_direction((float)(kExact ? __ldg(tag + i) : __float_as_uint(p.w)));
+}
+
+// One dynamic neighbour: pressure force dir (p_i + p_j) W1 and viscosity
+// (v_j - v_i) W2 (SF:567-589).  Pairs at r >= h add nothing in the
+// reference (the kernels return 0) and are skipped.  kExact follows the
+// reference's operations one for one: dir / r by true division, each
+// product rounded, no fused multiply-adds.
+template <bool kExact>
 __device__ __forceinline__ void add_dynamic_pair(PairSums& s, const float4& p, const float4& v, float pi, float h,
-                                                 const float4& q, const float4& u)
+                                                 const float4& q, const float4& u, const uint32_t* tag, uint32_t i)
 {
     float dx = __fsub_rn(q.x, p.x), dy = __fsub_rn(q.y, p.y), dz = __fsub_rn(q.z, p.z);
-    const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+    const float r2 = kExact ? __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz))
+                            : __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
     const float r = __fsqrt_rn(r2);
     if (!(r < h)) return;
     if (r2 == 0.f || r == 0.f) {
-        const float3 d = random_direction((float)__float_as_uint(p.w));
+        const float3 d = coincident_direction<kExact>(p, tag, i);
         dx = d.x; dy = d.y; dz = d.z;
+    } else if (kExact) {
+        dx = __fdiv_rn(dx, r); dy = __fdiv_rn(dy, r); dz = __fdiv_rn(dz, r);
     } else {
         const float inv = __frcp_rn(r);
         dx = __fmul_rn(dx, inv); dy = __fmul_rn(dy, inv); dz = __fmul_rn(dz, inv);
@@ -752,38 +781,64 @@ __device__ __forceinline__ void add_dynamic_pair(PairSums& s, const float4& p, c
     const float w = __fsub_rn(h, r);
     const float w1 = __fmul_rn(__fmul_rn(-3.f, w), w);
     const float w2 = __fmul_rn(6.f, w);
-    const float pp = __fmul_rn(__fadd_rn(pi, u.w), w1);
-    s.fp.x = __fmaf_rn(dx, pp, s.fp.x);
-    s.fp.y = __fmaf_rn(dy, pp, s.fp.y);
-    s.fp.z = __fmaf_rn(dz, pp, s.fp.z);
-    s.fv.x = __fmaf_rn(__fsub_rn(u.x, v.x), w2, s.fv.x);
-    s.fv.y = __fmaf_rn(__fsub_rn(u.y, v.y), w2, s.fv.y);
-    s.fv.z = __fmaf_rn(__fsub_rn(u.z, v.z), w2, s.fv.z);
+    const float pij = __fadd_rn(pi, u.w);
+    if (kExact) {
+        s.fp.x = __fadd_rn(s.fp.x, __fmul_rn(__fmul_rn(dx, pij), w1));
+        s.fp.y = __fadd_rn(s.fp.y, __fmul_rn(__fmul_rn(dy, pij), w1));
+        s.fp.z = __fadd_rn(s.fp.z, __fmul_rn(__fmul_rn(dz, pij), w1));
+        s.fv.x = __fadd_rn(s.fv.x, __fmul_rn(__fsub_rn(u.x, v.x), w2));
+        s.fv.y = __fadd_rn(s.fv.y, __fmul_rn(__fsub_rn(u.y, v.y), w2));
+        s.fv.z = __fadd_rn(s.fv.z, __fmul_rn(__fsub_rn(u.z, v.z), w2));
+    } else {
+        const float pp = __fmul_rn(pij, w1);
+        s.fp.x = __fmaf_rn(dx, pp, s.fp.x);
+        s.fp.y = __fmaf_rn(dy, pp, s.fp.y);
+        s.fp.z = __fmaf_rn(dz, pp, s.fp.z);
+        s.fv.x = __fmaf_rn(__fsub_rn(u.x, v.x), w2, s.fv.x);
+        s.fv.y = __fmaf_rn(__fsub_rn(u.y, v.y), w2, s.fv.y);
+        s.fv.z = __fmaf_rn(__fsub_rn(u.z, v.z), w2, s.fv.z);
+    }
 }
 
-__device__ __forceinline__ void add_static_pair(PairSums& s, const float4& p, float api, float h, const float4& q)
+// One static neighbour: dir |p_i| W1 (SF:600-622).  The reference also sums a
+// static viscosity term and multiplies it by 0 (SF:629): for finite values
+// that adds a signed zero to a force that is never -0, so it is omitted.
+template <bool kExact>
+__device__ __forceinline__ void add_static_pair(PairSums& s, const float4& p, float api, float h, const float4& q,
+                                                const uint32_t* tag, uint32_t i)
 {
     float dx = __fsub_rn(q.x, p.x), dy = __fsub_rn(q.y, p.y), dz = __fsub_rn(q.z, p.z);
-    const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+    const float r2 = kExact ? __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz))
+                            : __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
     const float r = __fsqrt_rn(r2);
     if (!(r < h)) return;
     if (r2 == 0.f || r == 0.f) {
-        const float3 d = random_direction((float)__float_as_uint(p.w));
+        const float3 d = coincident_direction<kExact>(p, tag, i);
         dx = d.x; dy = d.y; dz = d.z;
+    } else if (kExact) {
+        dx = __fdiv_rn(dx, r); dy = __fdiv_rn(dy, r); dz = __fdiv_rn(dz, r);
     } else {
         const float inv = __frcp_rn(r);
         dx = __fmul_rn(dx, inv); dy = __fmul_rn(dy, inv); dz = __fmul_rn(dz, inv);
     }
     const float w = __fsub_rn(h, r);
-    const float pp = __fmul_rn(api, __fmul_rn(__fmul_rn(-3.f, w), w));
-    s.fs.x = __fmaf_rn(dx, pp, s.fs.x);
-    s.fs.y = __fmaf_rn(dy, pp, s.fs.y);
-    s.fs.z = __fmaf_rn(dz, pp, s.fs.z);
+    const float w1 = __fmul_rn(__fmul_rn(-3.f, w), w);
+    if (kExact) {
+        s.fs.x = __fadd_rn(s.fs.x, __fmul_rn(__fmul_rn(dx, api), w1));
+        s.fs.y = __fadd_rn(s.fs.y, __fmul_rn(__fmul_rn(dy, api), w1));
+        s.fs.z = __fadd_rn(s.fs.z, __fmul_rn(__fmul_rn(dz, api), w1));
+    } else {
+        const float pp = __fmul_rn(api, w1);
+        s.fs.x = __fmaf_rn(dx, pp, s.fs.x);
+        s.fs.y = __fmaf_rn(dy, pp, s.fs.y);
+        s.fs.z = __fmaf_rn(dz, pp, s.fs.z);
+    }
 }
 
 // SF:626-645: scale the sums, add triangle forces and gravity, integrate,
-// store the moved particle and its new key.
-template <bool kRecordAccel>
+// store the moved particle and its new key.  The reference starts the total
+// from a zero vector (SF:631-635); kExact keeps that first add.
+template <bool kRecordAccel, bool kExact>
 __device__ __forceinline__ uint32_t integrate_particle(const SceneDesc& sc, uint32_t i, const float4& p, const float4& v,
                                                        float rho, const PairSums& s, const float* __restrict__ tris,
                                                        float4* __restrict__ pos_out, float4* __restrict__ vel_out,
@@ -792,9 +847,13 @@ __device__ __forceinline__ uint32_t integrate_particle(const SceneDesc& sc, uint
     const float s1 = __fmul_rn(__fdiv_rn(sc.mass, __fmul_rn(2.f, rho)), sc.kc);
     const float s2 = __fmul_rn(__fmul_rn(sc.visc, sc.mass), sc.kc);
     float3 f;
-    f.x = __fadd_rn(__fadd_rn(__fmul_rn(s.fp.x, s1), __fmul_rn(s.fv.x, s2)), __fmul_rn(s.fs.x, s1));
-    f.y = __fadd_rn(__fadd_rn(__fmul_rn(s.fp.y, s1), __fmul_rn(s.fv.y, s2)), __fmul_rn(s.fs.y, s1));
-    f.z = __fadd_rn(__fadd_rn(__fmul_rn(s.fp.z, s1), __fmul_rn(s.fv.z, s2)), __fmul_rn(s.fs.z, s1));
+    const float z = 0.f;
+    f.x = kExact ? __fadd_rn(z, __fmul_rn(s.fp.x, s1)) : __fmul_rn(s.fp.x, s1);
+    f.y = kExact ? __fadd_rn(z, __fmul_rn(s.fp.y, s1)) : __fmul_rn(s.fp.y, s1);
+    f.z = kExact ? __fadd_rn(z, __fmul_rn(s.fp.z, s1)) : __fmul_rn(s.fp.z, s1);
+    f.x = __fadd_rn(__fadd_rn(f.x, __fmul_rn(s.fv.x, s2)), __fmul_rn(s.fs.x, s1));
+    f.y = __fadd_rn(__fadd_rn(f.y, __fmul_rn(s.fv.y, s2)), __fmul_rn(s.fs.y, s1));
+    f.z = __fadd_rn(__fadd_rn(f.z, __fmul_rn(s.fv.z, s2)), __fmul_rn(s.fs.z, s1));
     for (uint32_t t = 0; t < sc.t; ++t) {
         const float3 tf = triangle_force(make_float3(p.x, p.y, p.z), tris + 9u * (sc.t_off + t));
         f.x = __fadd_rn(f.x, tf.x); f.y = __fadd_rn(f.y, tf.y); f.z = __fadd_rn(f.z, tf.z);
@@ -818,13 +877,21 @@ __device__ __forceinline__ uint32_t integrate_particle(const SceneDesc& sc, uint
     return k;
 }
 
-template <bool kRecordAccel>
+// Where the force pass writes and counts.
+struct ForceOut {
+    float4* pos_out;
+    float4* vel_out;
+    uint32_t* key_out;
+    uint32_t* arrival;
+    uint32_t* count;
+    float4* accel;
+};
+
+template <bool kRecordAccel, bool kExact>
 __device__ __forceinline__ void force_tile(const Tile& tile, const SceneDesc* scenes, const float4* __restrict__ pos,
-                                           const float4* __restrict__ vel, const float4* __restrict__ spos,
-                                           const float* __restrict__ tris, const NbrArgs& nl,
-                                           float4* __restrict__ pos_out, float4* __restrict__ vel_out,
-                                           uint32_t* __restrict__ key_out, uint32_t* __restrict__ arrival,
-                                           uint32_t* count, float4* accel)
+                                           const float4* __restrict__ vel, const uint32_t* __restrict__ tag,
+                                           const StaticTables& st, const float* __restrict__ tris, const NbrArgs& nl,
+                                           const ForceOut& o)
 {
     const SceneDesc& sc = scenes[tile.scene];
     const uint32_t i = tile.begin + threadIdx.x;
@@ -840,7 +907,7 @@ __device__ __forceinline__ void force_tile(const Tile& tile, const SceneDesc* sc
             const float4 p = pos[i];
             const float4 v = vel[i];
             const float pi = v.w;
-            const float rho = __fadd_rn(__fdiv_rn(pi, sc.gas), sc.rho0);
+            const float rho = __fadd_rn(__fdiv_rn(pi, sc.gas), sc.rho0);   // SF:541
             const uint32_t stride = nl.stride;
             PairSums s;
             s.fp = s.fv = s.fs = make_float3(0.f, 0.f, 0.f);
@@ -852,38 +919,34 @@ __device__ __forceinline__ void force_tile(const Tile& tile, const SceneDesc* sc
                                j3 = __ldg(lp + 3 * (size_t)stride);
                 const float4 q0 = __ldg(pos + j0), q1 = __ldg(pos + j1), q2 = __ldg(pos + j2), q3 = __ldg(pos + j3);
                 const float4 u0 = __ldg(vel + j0), u1 = __ldg(vel + j1), u2 = __ldg(vel + j2), u3 = __ldg(vel + j3);
-                add_dynamic_pair(s, p, v, pi, h, q0, u0);
-                add_dynamic_pair(s, p, v, pi, h, q1, u1);
-                add_dynamic_pair(s, p, v, pi, h, q2, u2);
-                add_dynamic_pair(s, p, v, pi, h, q3, u3);
+                add_dynamic_pair<kExact>(s, p, v, pi, h, q0, u0, tag, i);
+                add_dynamic_pair<kExact>(s, p, v, pi, h, q1, u1, tag, i);
+                add_dynamic_pair<kExact>(s, p, v, pi, h, q2, u2, tag, i);
+                add_dynamic_pair<kExact>(s, p, v, pi, h, q3, u3, tag, i);
             }
             for (; k < cd; ++k, lp += stride) {
                 const uint32_t j = __ldg(lp);
-                add_dynamic_pair(s, p, v, pi, h, __ldg(pos + j), __ldg(vel + j));
+                add_dynamic_pair<kExact>(s, p, v, pi, h, __ldg(pos + j), __ldg(vel + j), tag, i);
             }
             const float api = fabsf(pi);
             lp = nl.snbr + i;
-            for (uint32_t k = 0; k < cs; ++k, lp += stride) {
-                const uint32_t e = __ldg(lp);
-                const float4 q = __ldg(spos + (e & kIndexMask));
-                for (uint32_t m = e >> kMultShift; m; --m) add_static_pair(s, p, api, h, q);
-            }
-            g = sc.q_off + integrate_particle<kRecordAccel>(sc, i, p, v, rho, s, tris, pos_out, vel_out, key_out, accel);
+            for (uint32_t k = 0; k < cs; ++k, lp += stride)
+                add_static_pair<kExact>(s, p, api, h, static_entry_pos(__ldg(lp), st), tag, i);
+            g = sc.q_off + integrate_particle<kRecordAccel, kExact>(sc, i, p, v, rho, s, tris, o.pos_out, o.vel_out,
+                                                                    o.key_out, o.accel);
         }
     }
-    const uint32_t r = warp_aggregated_increment(count, g, valid);
-    if (valid) arrival[i] = r;
+    const uint32_t r = warp_aggregated_increment(o.count, g, valid);
+    if (valid) o.arrival[i] = r;
 }
 
-// Overflow particles: the same sums, walking the 27 buckets directly.
-template <bool kRecordAccel>
-__device__ __forceinline__ void force_overflow_tile(const Tile& tile, const SceneDesc* scenes, const float4* __restrict__ pos,
-                                                    const float4* __restrict__ vel, const uint32_t* __restrict__ start,
-                                                    const float4* __restrict__ spos, const uint32_t* __restrict__ sstart,
-                                                    const float* __restrict__ tris, const NbrArgs& nl,
-                                                    float4* __restrict__ pos_out, float4* __restrict__ vel_out,
-                                                    uint32_t* __restrict__ key_out, uint32_t* __restrict__ arrival,
-                                                    uint32_t* count, float4* accel)
+// Overflow particles: the same sums, walking the 27 cells directly.
+template <bool kRecordAccel, bool kExact>
+__device__ __forceinline__ void force_overflow_tile(const Tile& tile, const SceneDesc* scenes,
+                                                    const float4* __restrict__ pos, const float4* __restrict__ vel,
+                                                    const uint32_t* __restrict__ tag, const uint32_t* __restrict__ start,
+                                                    const StaticTables& st, const float* __restrict__ tris,
+                                                    const NbrArgs& nl, const ForceOut& o)
 {
     const SceneDesc& sc = scenes[tile.scene];
     const uint32_t i = tile.begin + threadIdx.x;
@@ -894,50 +957,24 @@ __device__ __forceinline__ void force_overflow_tile(const Tile& tile, const Scen
         valid = (c & 0xFFFFu) == kOverflow || (c >> 16) == kOverflow;
     }
     if (valid) {
-        const float h = sc.h, h2 = sc.h2;
+        const float h = sc.h;
         const float4 p = pos[i];
         const float4 v = vel[i];
         const float pi = v.w;
         const float api = fabsf(pi);
         const float rho = __fadd_rn(__fdiv_rn(pi, sc.gas), sc.rho0);
-        const Neighbourhood nb = neighbourhood(p.x, p.y, p.z, h);
-        const uint32_t delta = sc.p_off - __ldg(start + sc.q_off);
-        const uint32_t sdelta = sc.s ? sc.s_off - __ldg(sstart + sc.sf_off) : 0u;
-        const bool span_s_dup = nb_span(nb) >= sc.s;
+        const Walk w = make_walk<kExact>(sc, p, st.sbitmap);
         PairSums s;
         s.fp = s.fv = s.fs = make_float3(0.f, 0.f, 0.f);
-#pragma unroll 1
-        for (int a = 0; a < 3; ++a)
-#pragma unroll 1
-            for (int b = 0; b < 3; ++b)
-#pragma unroll 1
-                for (int c = 0; c < 3; ++c) {
-                    const uint32_t hsh = neighbour_hash(nb, a, b, c);
-                    const uint32_t bk = sc.q_off + fast_mod(hsh, sc.fm_b);
-                    const uint32_t beg = max(__ldg(start + bk) + delta, sc.p_off);
-                    const uint32_t end = min(__ldg(start + bk + 1) + delta, sc.p_off + sc.n);
-                    for (uint32_t j = beg; j < end; ++j) {
-                        const float4 q = __ldg(pos + j);
-                        if (dist2(q, p) <= h2 && j != i) add_dynamic_pair(s, p, v, pi, h, q, __ldg(vel + j));
-                    }
-                    if (sc.s) {
-                        const uint32_t sb = sc.sf_off + fast_mod(hsh, sc.fm_sf);
-                        const uint32_t sbeg = max(__ldg(sstart + sb) + sdelta, sc.s_off);
-                        const uint32_t send = min(__ldg(sstart + sb + 1) + sdelta, sc.s_off + sc.s);
-                        uint32_t mult = 0;
-                        for (uint32_t j = sbeg; j < send; ++j) {
-                            const float4 q = __ldg(spos + j);
-                            if (__float_as_uint(q.w) == hsh && dist2(q, p) <= h2) {
-                                if (!mult) mult = span_s_dup ? static_multiplicity(nb, sc.fm_s, hsh) : 1u;
-                                for (uint32_t m = mult; m; --m) add_static_pair(s, p, api, h, q);
-                            }
-                        }
-                    }
-                }
-        g = sc.q_off + integrate_particle<kRecordAccel>(sc, i, p, v, rho, s, tris, pos_out, vel_out, key_out, accel);
+        walk_neighbours<kExact>(
+            sc, i, p, w, pos, start, st,
+            [&](uint32_t j, const float4& q, float) { add_dynamic_pair<kExact>(s, p, v, pi, h, q, __ldg(vel + j), tag, i); },
+            [&](uint32_t, const float4& q, float) { add_static_pair<kExact>(s, p, api, h, q, tag, i); });
+        g = sc.q_off + integrate_particle<kRecordAccel, kExact>(sc, i, p, v, rho, s, tris, o.pos_out, o.vel_out,
+                                                                o.key_out, o.accel);
     }
-    const uint32_t r = warp_aggregated_increment(count, g, valid);
-    if (valid) arrival[i] = r;
+    const uint32_t r = warp_aggregated_increment(o.count, g, valid);
+    if (valid) o.arrival[i] = r;
 }
 
 }  // namespace sph

@@ -101,8 +101,9 @@ __global__ void __launch_bounds__(kTileThreads) k_na_scatter(NoAllocArgs a)
     a.scratch[kPermOff + slot] = i;
 }
 
-// Stable placement: particle j goes to its bucket's start plus the number of
-// the bucket's members with a smaller input index (gather_tile's rule).
+// Deterministic placement: particle j goes to its bucket's start plus the
+// number of the bucket's members with a larger input index, the order in
+// which the reference's counting sort fills a bucket (gather_tile's rule).
 __global__ void __launch_bounds__(kTileThreads) k_na_order(NoAllocArgs a)
 {
     const uint32_t j = blockIdx.x * kTileThreads + threadIdx.x;
@@ -113,7 +114,7 @@ __global__ void __launch_bounds__(kTileThreads) k_na_order(NoAllocArgs a)
     const uint32_t* perm = a.scratch + kPermOff;
     uint32_t rank = 0;
     if (e0 - b0 <= kStableRankLimit) {
-        for (uint32_t t = b0; t < e0; ++t) rank += perm[t] < j ? 1u : 0u;
+        for (uint32_t t = b0; t < e0; ++t) rank += perm[t] > j ? 1u : 0u;
     } else {
         rank = a.scratch[kArrivalOff + j];
     }

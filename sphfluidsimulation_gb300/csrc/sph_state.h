@@ -22,7 +22,12 @@ struct SortArgs {
     float4* vel_dst;
     uint32_t* key;
     uint32_t* arrival;
-    uint32_t* perm;
+    uint32_t* ptag;             // scatter slot -> tag
+    const uint32_t* tag_src;    // tag per source slot; null: the source slot itself
+    uint32_t* tag_dst;          // tag per sorted slot (unused with kTagNone)
+    uint32_t assign;            // TagAssign
+    const float4* accel_src;    // recorded acceleration per source slot, moved along (or null)
+    float4* accel_dst;
     uint32_t* count;
     uint32_t* start;
     uint32_t* err;
@@ -68,7 +73,19 @@ public:
     sph_status check_device_error();
 
     sph_status set_dt(uint32_t scene, float dt);
-    sph_status read_scene(uint32_t scene, sph_dynamic_particle* out, float* accel_out);
+    // Whether the steps queued next renumber the scene's buffer tags, as a
+    // reordering Update of the reference does (SimulationEngineCPU.cpp:441).
+    sph_status set_reorder(uint32_t scene, bool reorder);
+    // Neighbour-pass arithmetic: false fused/fast, true the reference's own.
+    void set_exact(bool exact)
+    {
+        if (exact != exact_ && graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+        if (exact != exact_) grid_cache_ = 0;
+        exact_ = exact;
+    }
+    bool exact() const { return exact_; }
+    // Caller's order, or with buffer_order the reference's buffer order (by tag).
+    sph_status read_scene(uint32_t scene, sph_dynamic_particle* out, float* accel_out, bool buffer_order = false);
     sph_status write_scene(uint32_t scene, const sph_dynamic_particle* in);
     sph_status read_static(uint32_t scene, sph_static_particle* out, uint32_t* bucket_starts);
     sph_status read_buckets(uint32_t scene, uint32_t* bucket_starts, uint32_t* slot_ids);
@@ -120,7 +137,9 @@ public:
     Tile* d_tiles = nullptr;
     Tile* d_stiles = nullptr;
     float4 *pos = nullptr, *vel = nullptr, *pos_tmp = nullptr, *vel_tmp = nullptr;
-    uint32_t *key = nullptr, *arrival = nullptr, *perm = nullptr, *count = nullptr, *start = nullptr;
+    uint32_t *key = nullptr, *arrival = nullptr, *ptag = nullptr, *count = nullptr, *start = nullptr;
+    uint32_t* tag = nullptr;       // buffer tag per sorted slot
+    uint32_t* tag_io = nullptr;    // tags in caller's order while a write re-sorts
     unsigned long long* scan_status = nullptr;
     uint32_t* scan_ticket = nullptr;
     uint32_t* err = nullptr;
@@ -136,7 +155,8 @@ public:
     uint32_t* sbitmap = nullptr;   // static-presence bitmaps (words)
     SceneDesc* d_sfscenes = nullptr;
     float* tris = nullptr;
-    float4* accel = nullptr;
+    float4* accel = nullptr;       // recorded acceleration per sorted slot
+    float4* accel_tmp = nullptr;   // as the force pass writes it (per tmp slot)
     float4* accel_io = nullptr;
     float4* staging = nullptr;
 
@@ -144,7 +164,7 @@ private:
     // sort kinds: 0 dynamic, 1 statics by the reference's table, 2 statics by
     // the neighbour-pass table
     sph_status enqueue_load(const float4* src, bool statics);
-    sph_status enqueue_sort(int kind);
+    sph_status enqueue_sort(int kind, bool keep_tags = false);
     sph_status enqueue_scan(uint32_t* cnt, uint32_t* out, uint32_t len);
     sph_status alloc_arrays(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s, uint32_t cap_sq, uint32_t cap_sf,
                             uint32_t cap_sbm, uint32_t cap_t, uint32_t max_scenes, uint32_t max_tiles);
@@ -152,6 +172,8 @@ private:
     sph_status enqueue_step_persistent();
     sph_status ensure_events();
     SortArgs sort_args(int kind) const;
+    template <bool kExact>
+    sph_status launch_step_staged(bool record_accel, bool timed);
     StepArgs step_args() const;
 
     int device_ = 0;
@@ -160,6 +182,7 @@ private:
     cudaEvent_t events_[6] = {};
     float stage_ms_[5] = {};
     uint32_t persistent_ctas_ = 0;
+    bool exact_ = false;
     uint32_t grid_cache_ = 0;
     uint32_t cap_n_ = 0, cap_q_ = 0, cap_s_ = 0, cap_sq_ = 0, cap_sf_ = 0, cap_sbm_ = 0, cap_t_ = 0, max_scenes_ = 0,
              max_tiles_ = 0;
@@ -168,6 +191,7 @@ private:
     float4* saved_pos_ = nullptr;          // save_state() copies
     float4* saved_vel_ = nullptr;
     uint32_t* saved_start_ = nullptr;
+    uint32_t* saved_tag_ = nullptr;
     SceneDesc* d_tmp_scene_ = nullptr;     // its dynamic and two static views
 };
 

@@ -5,8 +5,8 @@
 //   density  (vel.w = pressure)                      reference SF:358-501
 //   force    (tmp = integrated particles, key, count) reference SF:503-656
 //   scan     (start = exclusive scan of count)        reference SF:227-294 / ECPU:245-253
-//   scatter  (perm[start+arrival] = tmp slot)         reference SF:346-356
-//   gather   (stable rank, tmp -> sorted state)       reference SF:332-345
+//   scatter  (ptag[start+arrival] = buffer tag)       reference SF:346-356
+//   gather   (rank by tag, tmp -> sorted state)       reference SF:332-345
 // either as five launches (captured once in a CUDA graph) or as one
 // persistent cooperative launch with four bounded grid barriers.
 #include "sph_state.h"
@@ -37,13 +37,13 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(uint32_t* count, uint32_t
 
 __global__ void __launch_bounds__(kTileThreads) k_scatter(SortArgs a)
 {
-    scatter_tile(a.tiles[blockIdx.x], a.scenes, a.key, a.arrival, a.start, a.perm, a.err);
+    scatter_tile(a.tiles[blockIdx.x], a.scenes, a.key, a.arrival, a.start, a.tag_src, a.ptag, a.err);
 }
 
 __global__ void __launch_bounds__(kTileThreads) k_gather(SortArgs a)
 {
-    gather_tile(a.tiles[blockIdx.x], a.scenes, a.key, a.arrival, a.perm, a.start, a.pos_src, a.vel_src,
-                a.pos_dst, a.vel_dst, a.err);
+    gather_tile(a.tiles[blockIdx.x], a.scenes, a.key, a.arrival, a.ptag, a.start, a.pos_src, a.vel_src,
+                a.pos_dst, a.vel_dst, a.tag_dst, a.assign, a.err, a.accel_src, a.accel_dst);
 }
 
 __device__ __forceinline__ NbrArgs nbr_args(const StepArgs& a)
@@ -51,27 +51,38 @@ __device__ __forceinline__ NbrArgs nbr_args(const StepArgs& a)
     return NbrArgs{a.nbr, a.snbr, a.ncount, a.tile_overflow, a.nbr_stride};
 }
 
-__global__ void __launch_bounds__(kDensityThreads, SPH_DENSITY_MIN_CTAS) k_density(StepArgs a)
+__device__ __forceinline__ StaticTables static_tables(const StepArgs& a)
 {
-    density_tile(blockIdx.x, a.tiles[blockIdx.x], threadIdx.x, a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart,
-                 a.sbitmap, nbr_args(a));
+    return StaticTables{a.spos, a.sstart, a.spos_ref, a.sstart_ref, a.sbitmap};
 }
 
-template <bool kRecord>
+__device__ __forceinline__ ForceOut force_out(const StepArgs& a)
+{
+    return ForceOut{a.pos_tmp, a.vel_tmp, a.key, a.arrival, a.count, a.accel};
+}
+
+template <bool kExact>
+__global__ void __launch_bounds__(kDensityThreads, SPH_DENSITY_MIN_CTAS) k_density(StepArgs a)
+{
+    density_tile<kExact>(blockIdx.x, a.tiles[blockIdx.x], threadIdx.x, a.scenes, a.pos, a.vel, a.start,
+                         static_tables(a), nbr_args(a));
+}
+
+template <bool kRecord, bool kExact>
 __global__ void __launch_bounds__(kTileThreads, SPH_FORCE_MIN_CTAS) k_force(StepArgs a)
 {
-    force_tile<kRecord>(a.tiles[blockIdx.x], a.scenes, a.pos, a.vel, a.spos, a.tris, nbr_args(a), a.pos_tmp, a.vel_tmp,
-                        a.key, a.arrival, a.count, a.accel);
+    force_tile<kRecord, kExact>(a.tiles[blockIdx.x], a.scenes, a.pos, a.vel, a.tag, static_tables(a), a.tris,
+                                nbr_args(a), force_out(a));
 }
 
 // Particles whose neighbour list overflowed; whole tiles without one exit at
 // once (the density pass records a per-tile flag).
-template <bool kRecord>
+template <bool kRecord, bool kExact>
 __global__ void __launch_bounds__(kTileThreads) k_force_overflow(StepArgs a)
 {
     if (a.tile_overflow[blockIdx.x] == 0u) return;
-    force_overflow_tile<kRecord>(a.tiles[blockIdx.x], a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart, a.tris,
-                                 nbr_args(a), a.pos_tmp, a.vel_tmp, a.key, a.arrival, a.count, a.accel);
+    force_overflow_tile<kRecord, kExact>(a.tiles[blockIdx.x], a.scenes, a.pos, a.vel, a.tag, a.start,
+                                         static_tables(a), a.tris, nbr_args(a), force_out(a));
     __syncthreads();
     if (threadIdx.x == 0) a.tile_overflow[blockIdx.x] = 0u;   // every thread has read the flag
 }
@@ -105,6 +116,7 @@ __device__ __forceinline__ void grid_barrier(uint32_t* count, uint32_t* gen, uin
 // grid barrier between stages.  Tiles are taken grid-stride; scan tiles are
 // taken in increasing order per CTA, so every look-back waits only on a tile
 // a co-resident CTA reaches first.
+template <bool kExact>
 __global__ void __launch_bounds__(kTileThreads) k_step_persistent(StepArgs a, uint32_t scan_tiles)
 {
     __shared__ ScanSmem sm;
@@ -113,15 +125,15 @@ __global__ void __launch_bounds__(kTileThreads) k_step_persistent(StepArgs a, ui
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < scan_tiles; t += gridDim.x * blockDim.x)
         a.scan_status[t] = 0ull;
     const NbrArgs nl = nbr_args(a);
+    const StaticTables st = static_tables(a);
+    const ForceOut fo = force_out(a);
     for (uint32_t t = blockIdx.x; t < a.num_tiles; t += gridDim.x)
-        density_tile(t, a.tiles[t], threadIdx.x, a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart, a.sbitmap, nl);
+        density_tile<kExact>(t, a.tiles[t], threadIdx.x, a.scenes, a.pos, a.vel, a.start, st, nl);
     grid_barrier(a.bar_count, a.bar_gen, a.err);
     for (uint32_t t = blockIdx.x; t < a.num_tiles; t += gridDim.x) {
-        force_tile<false>(a.tiles[t], a.scenes, a.pos, a.vel, a.spos, a.tris, nl, a.pos_tmp, a.vel_tmp, a.key,
-                          a.arrival, a.count, a.accel);
+        force_tile<false, kExact>(a.tiles[t], a.scenes, a.pos, a.vel, a.tag, st, a.tris, nl, fo);
         if (a.tile_overflow[t]) {
-            force_overflow_tile<false>(a.tiles[t], a.scenes, a.pos, a.vel, a.start, a.spos, a.sstart, a.tris, nl,
-                                       a.pos_tmp, a.vel_tmp, a.key, a.arrival, a.count, a.accel);
+            force_overflow_tile<false, kExact>(a.tiles[t], a.scenes, a.pos, a.vel, a.tag, a.start, st, a.tris, nl, fo);
             __syncthreads();
             if (threadIdx.x == 0) a.tile_overflow[t] = 0u;
         }
@@ -131,11 +143,11 @@ __global__ void __launch_bounds__(kTileThreads) k_step_persistent(StepArgs a, ui
         scan_tile(t, a.count, a.start, a.scan_len, a.scan_status, a.err, sm);
     grid_barrier(a.bar_count, a.bar_gen, a.err);
     for (uint32_t t = blockIdx.x; t < a.num_tiles; t += gridDim.x)
-        scatter_tile(a.tiles[t], a.scenes, a.key, a.arrival, a.start, a.perm, a.err);
+        scatter_tile(a.tiles[t], a.scenes, a.key, a.arrival, a.start, a.tag, a.ptag, a.err);
     grid_barrier(a.bar_count, a.bar_gen, a.err);
     for (uint32_t t = blockIdx.x; t < a.num_tiles; t += gridDim.x)
-        gather_tile(a.tiles[t], a.scenes, a.key, a.arrival, a.perm, a.start, a.pos_tmp, a.vel_tmp, a.pos, a.vel,
-                    a.err);
+        gather_tile(a.tiles[t], a.scenes, a.key, a.arrival, a.ptag, a.start, a.pos_tmp, a.vel_tmp, a.pos, a.vel,
+                    a.tag, kTagStep, a.err);
 }
 
 __global__ void __launch_bounds__(kTileThreads) k_static_bitmap(const Tile* tiles, const SceneDesc* scenes,
@@ -144,11 +156,14 @@ __global__ void __launch_bounds__(kTileThreads) k_static_bitmap(const Tile* tile
     static_bitmap_tile(tiles[blockIdx.x], scenes, spos, sbitmap);
 }
 
-// Readback: sorted slot i -> caller's order, in the reference's 32-byte layout
-// (Particles.h:9-17); hash = key of the position (SF:644-645).
+// Readback: sorted slot i -> caller's order (or, with by_tag, the reference's
+// buffer order), in the reference's 32-byte layout (Particles.h:9-17); hash =
+// key of the position (SF:644-645).  Optionally the acceleration and the
+// buffer tag move along.
 __global__ void __launch_bounds__(kTileThreads) k_unsort(const Tile* tiles, const SceneDesc* scenes, const float4* pos,
                                                          const float4* vel, float4* out, const float4* accel_in,
-                                                         float4* accel_out)
+                                                         float4* accel_out, const uint32_t* tag_in, uint32_t* tag_out,
+                                                         int by_tag)
 {
     const Tile tile = tiles[blockIdx.x];
     const SceneDesc& sc = scenes[tile.scene];
@@ -156,13 +171,14 @@ __global__ void __launch_bounds__(kTileThreads) k_unsort(const Tile* tiles, cons
     if (i >= tile.end) return;
     const float4 p = pos[i];
     const float4 v = vel[i];
-    const uint32_t id = __float_as_uint(p.w);
+    const uint32_t id = by_tag ? tag_in[i] : __float_as_uint(p.w);
     if (id >= sc.n) return;
     const uint32_t key = fast_mod(cell_hash(p.x, p.y, p.z, sc.h), sc.fm_b);
     const uint32_t o = sc.p_off + id;
     out[2 * (size_t)o] = make_float4(p.x, p.y, p.z, v.w);
     out[2 * (size_t)o + 1] = make_float4(v.x, v.y, v.z, __uint_as_float(key));
     if (accel_in) accel_out[o] = accel_in[i];
+    if (tag_out) tag_out[o] = tag_in[i];
 }
 
 // Upload staging (caller's order, positions and velocities as float4 pairs)
@@ -217,21 +233,22 @@ void StepState::release()
 {
     if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
     void* ptrs[] = {d_scenes, d_sscenes, d_sfscenes, d_tiles, d_stiles, pos, vel, pos_tmp, vel_tmp, key, arrival,
-                    perm, count, start, scan_status, scan_ticket, err, bar, spos, sstart, spos_ref, sstart_ref, tris,
-                    accel, accel_io, staging, d_tmp_tiles_, d_tmp_scene_, nbr, snbr, ncount, tile_overflow,
-                    saved_pos_, saved_vel_, saved_start_, sbitmap};
+                    ptag, count, start, scan_status, scan_ticket, err, bar, spos, sstart, spos_ref, sstart_ref, tris,
+                    accel, accel_tmp, accel_io, staging, d_tmp_tiles_, d_tmp_scene_, nbr, snbr, ncount, tile_overflow,
+                    saved_pos_, saved_vel_, saved_start_, sbitmap, tag, tag_io, saved_tag_};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     d_scenes = d_sscenes = d_sfscenes = d_tmp_scene_ = nullptr;
     saved_pos_ = saved_vel_ = nullptr;
     saved_start_ = nullptr;
+    tag = tag_io = saved_tag_ = nullptr;
     grid_cache_ = 0;
     spos_ref = nullptr;
     sstart_ref = nbr = snbr = ncount = tile_overflow = sbitmap = nullptr;
     d_tiles = d_stiles = d_tmp_tiles_ = nullptr;
-    pos = vel = pos_tmp = vel_tmp = spos = accel = accel_io = nullptr;
+    pos = vel = pos_tmp = vel_tmp = spos = accel = accel_tmp = accel_io = nullptr;
     staging = nullptr;
-    key = arrival = perm = count = start = scan_ticket = err = bar = sstart = nullptr;
+    key = arrival = ptag = count = start = scan_ticket = err = bar = sstart = nullptr;
     scan_status = nullptr;
     tris = nullptr;
     for (auto& e : events_)
@@ -347,7 +364,9 @@ sph_status StepState::alloc_arrays(uint32_t cap_n, uint32_t cap_q, uint32_t cap_
     ALLOC(vel_tmp, work_n);
     ALLOC(key, work_n);
     ALLOC(arrival, work_n);
-    ALLOC(perm, work_n);
+    ALLOC(ptag, work_n);
+    ALLOC(tag, cap_n);
+    ALLOC(tag_io, cap_n);
     ALLOC(count, cnt_len);
     ALLOC(start, cap_q + 1ull);
     ALLOC(scan_status, scan_tiles_max);
@@ -537,7 +556,9 @@ sph_status StepState::grow_arena(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s,
     GROW(vel_tmp, old_work, new_work, false);
     GROW(key, old_work, new_work, false);
     GROW(arrival, old_work, new_work, false);
-    GROW(perm, old_work, new_work, false);
+    GROW(ptag, old_work, new_work, false);
+    GROW(tag, cap_n_, cap_n, false);
+    GROW(tag_io, 0, cap_n, false);
     GROW(staging, 2 * old_work, 2 * new_work, false);
     GROW(count, old_cnt, new_cnt, true);
     GROW(start, cap_q_ + 1ull, cap_q + 1ull, false);
@@ -556,6 +577,7 @@ sph_status StepState::grow_arena(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s,
     GROW(d_stiles, 0, tiles_for(cap_n) + max_scenes_, false);
 #undef GROW
     if (accel) { cudaFree(accel); accel = nullptr; }
+    if (accel_tmp) { cudaFree(accel_tmp); accel_tmp = nullptr; }
     if (accel_io) { cudaFree(accel_io); accel_io = nullptr; }
     max_tiles_ = tiles_for(cap_n) + max_scenes_;
     cap_n_ = cap_n;
@@ -670,6 +692,9 @@ sph_status StepState::enqueue_load(const float4* src, bool statics)
     return SPH_OK;
 }
 
+// The sorts outside a step: kind 0 loads dynamic particles (the initial
+// sort numbers their tags by slot, like the reference's initial reorder,
+// SimulationEngineCPU.cpp:69-128), kinds 1 and 2 statics (no tags).
 SortArgs StepState::sort_args(int kind) const
 {
     SortArgs a{};
@@ -681,7 +706,10 @@ SortArgs StepState::sort_args(int kind) const
     a.vel_dst = kind == 0 ? vel : staging;   // static velocities are discarded
     a.key = key;
     a.arrival = arrival;
-    a.perm = perm;
+    a.ptag = ptag;
+    a.tag_src = nullptr;
+    a.tag_dst = kind == 0 ? tag : nullptr;
+    a.assign = kind == 0 ? kTagSlot : kTagNone;
     a.count = count;
     a.start = kind == 0 ? start : (kind == 1 ? sstart_ref : sstart);
     a.err = err;
@@ -691,11 +719,15 @@ SortArgs StepState::sort_args(int kind) const
 // Counting sort of the tmp arrays into a sorted array: hash + count, scan,
 // scatter, stable gather (positions must already be in pos_tmp, and stay
 // there, so both static sorts read the same load).
-sph_status StepState::enqueue_sort(int kind)
+sph_status StepState::enqueue_sort(int kind, bool keep_tags)
 {
     const std::vector<Tile>& tl = kind == 0 ? tiles : stiles;
     if (tl.empty()) return SPH_OK;
     SortArgs a = sort_args(kind);
+    if (keep_tags) {   // a write between steps: every particle keeps its tag
+        a.tag_src = tag_io;
+        a.assign = kTagKeep;
+    }
     const uint32_t len = kind == 0 ? scan_len : (kind == 1 ? sscan_len : sfscan_len);
     const unsigned nt = (unsigned)tl.size();
     k_hash_count<<<nt, kTileThreads, 0, stream_>>>(a);
@@ -731,7 +763,8 @@ StepArgs StepState::step_args() const
     a.vel_tmp = vel_tmp;
     a.key = key;
     a.arrival = arrival;
-    a.perm = perm;
+    a.ptag = ptag;
+    a.tag = tag;
     a.count = count;
     a.start = start;
     a.scan_len = scan_len;
@@ -739,9 +772,11 @@ StepArgs StepState::step_args() const
     a.scan_ticket = scan_ticket;
     a.spos = spos;
     a.sstart = sstart;
+    a.spos_ref = spos_ref;
+    a.sstart_ref = sstart_ref;
     a.tris = tris;
     a.sbitmap = sbitmap;
-    a.accel = accel;
+    a.accel = accel_tmp;
     a.err = err;
     a.bar_count = bar;
     a.bar_gen = bar + 1;
@@ -760,24 +795,31 @@ sph_status StepState::ensure_events()
     return SPH_OK;
 }
 
-// One step as five launches (plus the scan's two memsets).  With `timed`,
+// One step as six launches (plus the scan's two memsets).  With `timed`,
 // events bracket each stage on the launching stream.
-sph_status StepState::enqueue_step_staged(bool record_accel, bool timed)
+template <bool kExact>
+sph_status StepState::launch_step_staged(bool record_accel, bool timed)
 {
-    if (tiles.empty()) return SPH_OK;
     const unsigned nt = (unsigned)tiles.size();
     StepArgs a = step_args();
     SortArgs s = sort_args(0);
+    s.tag_src = tag;          // the step's sort: tags per scene reorder flag
+    s.tag_dst = tag;
+    s.assign = kTagStep;
+    if (record_accel) {       // the recorded acceleration follows its particle
+        s.accel_src = accel_tmp;
+        s.accel_dst = accel;
+    }
     if (timed) CUDA_TRY(cudaEventRecord(events_[0], stream_));
-    k_density<<<nt, kDensityThreads, 0, stream_>>>(a);
+    k_density<kExact><<<nt, kDensityThreads, 0, stream_>>>(a);
     CUDA_TRY(cudaGetLastError());
     if (timed) CUDA_TRY(cudaEventRecord(events_[1], stream_));
     if (record_accel) {
-        k_force<true><<<nt, kTileThreads, 0, stream_>>>(a);
-        k_force_overflow<true><<<nt, kTileThreads, 0, stream_>>>(a);
+        k_force<true, kExact><<<nt, kTileThreads, 0, stream_>>>(a);
+        k_force_overflow<true, kExact><<<nt, kTileThreads, 0, stream_>>>(a);
     } else {
-        k_force<false><<<nt, kTileThreads, 0, stream_>>>(a);
-        k_force_overflow<false><<<nt, kTileThreads, 0, stream_>>>(a);
+        k_force<false, kExact><<<nt, kTileThreads, 0, stream_>>>(a);
+        k_force_overflow<false, kExact><<<nt, kTileThreads, 0, stream_>>>(a);
     }
     CUDA_TRY(cudaGetLastError());
     if (timed) CUDA_TRY(cudaEventRecord(events_[2], stream_));
@@ -793,6 +835,17 @@ sph_status StepState::enqueue_step_staged(bool record_accel, bool timed)
     return SPH_OK;
 }
 
+sph_status StepState::enqueue_step_staged(bool record_accel, bool timed)
+{
+    if (tiles.empty()) return SPH_OK;
+    return exact_ ? launch_step_staged<true>(record_accel, timed) : launch_step_staged<false>(record_accel, timed);
+}
+
+static const void* persistent_kernel(bool exact)
+{
+    return exact ? (const void*)k_step_persistent<true> : (const void*)k_step_persistent<false>;
+}
+
 sph_status StepState::persistent_grid(uint32_t* grid)
 {
     if (grid_cache_) {
@@ -801,7 +854,7 @@ sph_status StepState::persistent_grid(uint32_t* grid)
     }
     int sms = 0, per_sm = 0;
     CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
-    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step_persistent, kTileThreads, 0));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_kernel(exact_), kTileThreads, 0));
     if (per_sm < 1) per_sm = 1;
     uint32_t g = (uint32_t)(sms * per_sm);
     if (persistent_ctas_ && persistent_ctas_ < g) g = persistent_ctas_;
@@ -819,7 +872,7 @@ sph_status StepState::enqueue_step_persistent()
     StepArgs a = step_args();
     uint32_t scan_tiles = (scan_len + kScanTile - 1) / kScanTile;
     void* args[] = {&a, &scan_tiles};
-    CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_step_persistent, dim3(grid), dim3(kTileThreads), args, 0, stream_));
+    CUDA_TRY(cudaLaunchCooperativeKernel(persistent_kernel(exact_), dim3(grid), dim3(kTileThreads), args, 0, stream_));
     return SPH_OK;
 }
 
@@ -829,6 +882,8 @@ sph_status StepState::enqueue_steps(uint32_t steps, StepMode mode, bool record_a
     if (tiles.empty() || steps == 0) return SPH_OK;
     if (record_accel && !accel) {
         sph_status st = dev_alloc(&accel, total_n);
+        if (st != SPH_OK) return st;
+        st = dev_alloc(&accel_tmp, total_n);
         if (st != SPH_OK) return st;
         if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
     }
@@ -906,8 +961,20 @@ sph_status StepState::set_dt(uint32_t scene, float dt)
     return SPH_OK;
 }
 
+sph_status StepState::set_reorder(uint32_t scene, bool reorder)
+{
+    if (scene >= scenes.size()) return SPH_ERR_NOT_FOUND;
+    const uint32_t r = reorder ? 1u : 0u;
+    if (scenes[scene].reorder == r) return SPH_OK;
+    scenes[scene].reorder = r;
+    CUDA_TRY(cudaMemcpyAsync(&d_scenes[scene].reorder, &scenes[scene].reorder, sizeof(uint32_t), cudaMemcpyHostToDevice,
+                             stream_));
+    CUDA_TRY(cudaStreamSynchronize(stream_));
+    return SPH_OK;
+}
+
 // Reads one scene's particles (caller's order) into host `out` (n x 32 B).
-sph_status StepState::read_scene(uint32_t scene, sph_dynamic_particle* out, float* accel_out)
+sph_status StepState::read_scene(uint32_t scene, sph_dynamic_particle* out, float* accel_out, bool buffer_order)
 {
     if (scene >= scenes.size()) return SPH_ERR_NOT_FOUND;
     const SceneDesc& d = scenes[scene];
@@ -921,7 +988,8 @@ sph_status StepState::read_scene(uint32_t scene, sph_dynamic_particle* out, floa
     const uint32_t t1 = scene + 1 < tile_first_.size() ? tile_first_[scene + 1] : (uint32_t)tiles.size();
     if (t1 > t0)
         k_unsort<<<t1 - t0, kTileThreads, 0, stream_>>>(d_tiles + t0, d_scenes, pos, vel, staging,
-                                                        accel_out ? accel : nullptr, accel_io);
+                                                        accel_out ? accel : nullptr, accel_io, tag, nullptr,
+                                                        buffer_order ? 1 : 0);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaMemcpyAsync(out, staging + 2ull * d.p_off, sizeof(sph_dynamic_particle) * d.n, cudaMemcpyDeviceToHost, stream_));
     if (accel_out) {
@@ -945,13 +1013,15 @@ sph_status StepState::write_scene(uint32_t scene, const sph_dynamic_particle* in
     if (scene >= scenes.size()) return SPH_ERR_NOT_FOUND;
     const SceneDesc& d = scenes[scene];
     if (!d.n) return SPH_OK;
-    // move the current sorted state of all scenes into staging order first
-    k_unsort<<<(unsigned)tiles.size(), kTileThreads, 0, stream_>>>(d_tiles, d_scenes, pos, vel, staging, nullptr, nullptr);
+    // move the current sorted state of all scenes, and their buffer tags, into
+    // staging order first; the re-sort keeps every particle's tag
+    k_unsort<<<(unsigned)tiles.size(), kTileThreads, 0, stream_>>>(d_tiles, d_scenes, pos, vel, staging, nullptr, nullptr,
+                                                                   tag, tag_io, 0);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaMemcpyAsync(staging + 2ull * d.p_off, in, sizeof(sph_dynamic_particle) * d.n, cudaMemcpyHostToDevice, stream_));
     sph_status st = enqueue_load(staging, false);
     if (st != SPH_OK) return st;
-    st = enqueue_sort(0);
+    st = enqueue_sort(0, /*keep_tags=*/true);
     if (st != SPH_OK) return st;
     CUDA_TRY(cudaStreamSynchronize(stream_));
     return check_device_error();
@@ -1024,6 +1094,8 @@ sph_status StepState::save_state()
     if (!saved_pos_ && (st = dev_alloc(&saved_pos_, cap_n_)) != SPH_OK) return st;
     if (!saved_vel_ && (st = dev_alloc(&saved_vel_, cap_n_)) != SPH_OK) return st;
     if (!saved_start_ && (st = dev_alloc(&saved_start_, cap_q_ + 1ull)) != SPH_OK) return st;
+    if (!saved_tag_ && (st = dev_alloc(&saved_tag_, cap_n_)) != SPH_OK) return st;
+    CUDA_TRY(cudaMemcpyAsync(saved_tag_, tag, sizeof(uint32_t) * cap_n_, cudaMemcpyDeviceToDevice, stream_));
     CUDA_TRY(cudaMemcpyAsync(saved_pos_, pos, sizeof(float4) * cap_n_, cudaMemcpyDeviceToDevice, stream_));
     CUDA_TRY(cudaMemcpyAsync(saved_vel_, vel, sizeof(float4) * cap_n_, cudaMemcpyDeviceToDevice, stream_));
     CUDA_TRY(cudaMemcpyAsync(saved_start_, start, sizeof(uint32_t) * (cap_q_ + 1ull), cudaMemcpyDeviceToDevice, stream_));
@@ -1033,7 +1105,8 @@ sph_status StepState::save_state()
 
 sph_status StepState::restore_state()
 {
-    if (!saved_pos_ || !saved_vel_ || !saved_start_) return SPH_ERR_NOT_INITIALIZED;
+    if (!saved_pos_ || !saved_vel_ || !saved_start_ || !saved_tag_) return SPH_ERR_NOT_INITIALIZED;
+    CUDA_TRY(cudaMemcpyAsync(tag, saved_tag_, sizeof(uint32_t) * cap_n_, cudaMemcpyDeviceToDevice, stream_));
     CUDA_TRY(cudaMemcpyAsync(pos, saved_pos_, sizeof(float4) * cap_n_, cudaMemcpyDeviceToDevice, stream_));
     CUDA_TRY(cudaMemcpyAsync(vel, saved_vel_, sizeof(float4) * cap_n_, cudaMemcpyDeviceToDevice, stream_));
     CUDA_TRY(cudaMemcpyAsync(start, saved_start_, sizeof(uint32_t) * (cap_q_ + 1ull), cudaMemcpyDeviceToDevice, stream_));
@@ -1045,7 +1118,7 @@ sph_status StepState::persistent_capacity(uint32_t* sms, uint32_t* per_sm)
 {
     int s = 0, b = 0;
     CUDA_TRY(cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, device_));
-    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_step_persistent, kTileThreads, 0));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, persistent_kernel(exact_), kTileThreads, 0));
     *sms = (uint32_t)s;
     *per_sm = (uint32_t)std::max(b, 1);
     return SPH_OK;

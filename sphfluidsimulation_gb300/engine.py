@@ -118,6 +118,14 @@ class SimulationEngineCUDA:
         check(self.lib.sph_engine_read_dynamic(self.h, out.ctypes.data_as(C.c_void_p)), "sph_engine_read_dynamic")
         return out
 
+    def read_dynamic_buffer(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """The particles in the reference's buffer order (its LockRead bytes)."""
+        if out is None:
+            out = np.zeros(self.n, DYN_DTYPE)
+        check(self.lib.sph_engine_read_dynamic_buffer(self.h, out.ctypes.data_as(C.c_void_p)),
+              "sph_engine_read_dynamic_buffer")
+        return out
+
     def write_dynamic(self, particles: np.ndarray) -> None:
         p = np.ascontiguousarray(particles, DYN_DTYPE)
         check(self.lib.sph_engine_write_dynamic(self.h, p.ctypes.data_as(C.c_void_p)), "sph_engine_write_dynamic")
@@ -135,6 +143,11 @@ class SimulationEngineCUDA:
         ids = np.zeros(self.n, np.uint32)
         check(self.lib.sph_engine_read_buckets(self.h, _uptr(starts), _uptr(ids)), "sph_engine_read_buckets")
         return starts, ids
+
+    def set_exact(self, exact: bool = True) -> None:
+        """Neighbour-pass arithmetic: the reference's own operations (exact,
+        bit-identical to its synchronous CPU engine) or the fast fused form."""
+        check(self.lib.sph_engine_set_exact(self.h, int(exact)), "sph_engine_set_exact")
 
     def record_acceleration(self, on: bool = True) -> None:
         check(self.lib.sph_engine_record_acceleration(self.h, int(on)), "sph_engine_record_acceleration")

@@ -34,9 +34,15 @@ def golden_scenes():
     out.append((s, [1, 4, 15]))
     s = scenes.dam_break((10, 8, 12), 0.02, 0.04, (0.5, 0.4, 0.5), 0, mass=0.008, name="small_dam")
     out.append((s, [1, 9, 20]))
+    # reorderTimeInterval 0: the elapsed time is reset whenever it passes the
+    # interval, so the reference never reorders (SimulationEngineCPU.cpp:441,452-454)
     s = scenes.dam_break((10, 8, 12), 0.02, 0.04, (0.5, 0.4, 0.5), 0, mass=0.008, name="small_dam_reorder")
     s.reorder_interval = 0.0
     out.append((s, [1, 2, 3]))
+    # a negative interval reorders on every Update call
+    s = scenes.dam_break((10, 8, 12), 0.02, 0.04, (0.5, 0.4, 0.5), 0, mass=0.008, name="small_dam_reorder_each_call")
+    s.reorder_interval = -1.0
+    out.append((s, [1, 2, 5, 9]))
     # fluid block straddling the origin: negative cells on every axis
     s = scenes.dam_break((9, 7, 9), 0.02, 0.04, (0.4, 0.3, 0.4), 0, mass=0.008, name="negative_cells")
     s.dyn_pos = (s.dyn_pos - np.float32(0.09)).astype(np.float32)

@@ -136,8 +136,9 @@ class Oracle:
         return out
 
     def maps(self):
-        """(hash_map[B+1], particle_map[N], init_order[N]) -- init_order[slot]
-        is the input index of the particle in that buffer slot."""
+        """(hash_map[B+1], particle_map[N], order[N]) -- order[slot] is the
+        input index of the particle in that slot of the current buffer (the
+        init permutation until a reordering step permutes it)."""
         hm = np.zeros(self.buckets + 1, np.uint32)
         pm = np.zeros(self.n, np.uint32)
         io = np.zeros(self.n, np.uint32)
