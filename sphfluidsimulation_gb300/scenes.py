@@ -84,6 +84,7 @@ class Scene:
     triangles: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, 9), np.float32))
     dyn_vel: Optional[np.ndarray] = None
     reorder_interval: float = float(np.finfo(np.float32).max)
+    other_parameters: dict = dataclasses.field(default_factory=dict)   # the scene file's otherParameters
 
     @property
     def n(self) -> int:

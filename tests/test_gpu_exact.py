@@ -131,3 +131,33 @@ def test_exact_switch_back_to_fast():
     g = e.read_dynamic_buffer()
     r = o.read_raw()
     assert np.abs(g["pos"].astype(np.float64) - r["pos"]).max() < 1e-6
+
+
+def test_exact_scene_file_with_boundary_mesh(tmp_path):
+    """A scene in the reference's JSON format with an OBJ boundary mesh (a
+    floor quad and a tilted panel, 3 triangles) through the loader: the exact
+    engine equals the oracle, triangle forces included."""
+    import json
+    from sphfluidsimulation_gb300 import scene_json
+    (tmp_path / "panel.obj").write_text(
+        "o Floor\nv -0.1 -0.01 -0.1\nv 0.7 -0.01 -0.1\nv 0.7 -0.01 0.7\nv -0.1 -0.01 0.7\nf 1 2 3 4\n"
+        "o Panel\nv 0.3 0.0 0.0\nv 0.3 0.4 0.2\nv 0.6 0.0 0.5\nf 5 6 7\n")
+    doc = {
+        "particleBehaviourParameters": {"particleMass": 0.008, "gasConstant": 200, "elasticity": 0,
+                                        "viscosity": 0.1, "gravity": [0, -9.81, 0], "restDensity": 1000,
+                                        "maxInteractionDistance": 0.04},
+        "particleSetBlueprints": [
+            {"layerName": "dynamic", "particleSetBlueprintType": "FilledBox",
+             "properties": {"particlesPerUnit": 125000, "randomOffsetIntensity": 1, "seed": 3,
+                            "spawnVolumeOffset": [0.02, 0.02, 0.02], "spawnVolumeSize": [0.24, 0.2, 0.24]}},
+            {"layerName": "static", "particleSetBlueprintType": "BoxShell",
+             "properties": {"particleDistance": 0.02, "randomOffsetIntensity": 0,
+                            "spawnVolumeOffset": [0, 0, 0], "spawnVolumeSize": [0.6, 0.4, 0.6]}}],
+        "boundaryMesh": {"path": "panel.obj"},
+        "otherParameters": {"reorderTimeInterval": "-1"},
+    }
+    path = tmp_path / "scene.json"
+    path.write_text(json.dumps(doc))
+    sc = scene_json.load_scene(str(path), dt=1e-4)
+    assert sc.triangles.shape == (3, 9) and sc.n > 5000
+    run_against_oracle(sc, [1, 4, 10])
