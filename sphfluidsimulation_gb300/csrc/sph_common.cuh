@@ -123,7 +123,16 @@ struct SceneDesc {
     float self_density;
     float kc;       // smoothing kernel constant 15 / (3.1415 h^6)
     float dt;
+    // triangle cells (t > 0 and tg_nx > 0): cell (x, y, z) of point p is
+    // floor((p - tg_o) * tg_inv); its triangles are tri_list[tri_cells[c] ..
+    // tri_cells[c + 1]) with c = tg_cell_off + (z * tg_ny + y) * tg_nx + x
+    float tg_ox, tg_oy, tg_oz, tg_inv;
+    uint32_t tg_nx, tg_ny, tg_nz, tg_cell_off;
 };
+
+// Reach of a boundary triangle: CalculateTriangleForce returns zero beyond
+// this distance (SF:206, 214-215).
+constexpr float kTriangleReach = 2.5f;
 
 // A tile: up to one CTA's worth of consecutive slots of one scene.
 struct Tile {

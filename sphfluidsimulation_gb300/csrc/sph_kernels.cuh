@@ -67,6 +67,8 @@ struct StepArgs {
     const float4* spos_ref;     // static particles in the reference's own s-bucket order
     const uint32_t* sstart_ref; // its bucket table
     const float* tris;          // 9 floats per triangle
+    const uint32_t* tri_cells;  // triangle cells: list starts per cell (+1)
+    const uint32_t* tri_list;   // global triangle indices, increasing inside a cell
     const uint32_t* sbitmap;    // static-presence bitmaps of all scenes
     float4* accel;              // optional: acceleration per sorted slot (.w unused)
     uint32_t* err;              // device status word
@@ -187,8 +189,8 @@ __device__ __noinline__ inline float3 triangle_force(float3 p, const float* tri)
     }
     const float3 to = sub(q, p);
     const float dist = __fsqrt_rn(dot(to, to));
-    if (dist > 2.5f) return make_float3(0.f, 0.f, 0.f);
-    const float t = __fsub_rn(__fdiv_rn(1.f, __fdiv_rn(dist, 2.5f)), 1.f);
+    if (dist > kTriangleReach) return make_float3(0.f, 0.f, 0.f);
+    const float t = __fsub_rn(__fdiv_rn(1.f, __fdiv_rn(dist, kTriangleReach)), 1.f);
     const float amp = __fmul_rn(t, t);
     float3 dir = make_float3(__fdiv_rn(-to.x, dist), __fdiv_rn(-to.y, dist), __fdiv_rn(-to.z, dist));
     return make_float3(__fmul_rn(__fmul_rn(dir.x, amp), 50.f), __fmul_rn(__fmul_rn(dir.y, amp), 50.f),
@@ -838,9 +840,44 @@ __device__ __forceinline__ void add_static_pair(PairSums& s, const float4& p, fl
 // SF:626-645: scale the sums, add triangle forces and gravity, integrate,
 // store the moved particle and its new key.  The reference starts the total
 // from a zero vector (SF:631-635); kExact keeps that first add.
+// The boundary mesh and its triangle cells.
+struct TriangleMesh {
+    const float* tris;          // 9 floats per triangle
+    const uint32_t* cells;
+    const uint32_t* list;
+};
+
+// SF:636-637: the force of every triangle, added in triangle order.  With
+// triangle cells only the triangles listed for the particle's cell are
+// evaluated, still in increasing index: every other one lies beyond
+// kTriangleReach and adds the zero vector, which leaves the total as it is
+// (the total is never -0, as it starts from +0).  A point outside the cells
+// (or NaN) is beyond reach of every triangle.
+__device__ __forceinline__ void add_triangle_forces(const SceneDesc& sc, const TriangleMesh& tm, float3 p, float3& f)
+{
+    if (!sc.t) return;
+    auto add = [&](uint32_t t) {
+        const float3 tf = triangle_force(p, tm.tris + 9u * t);
+        f.x = __fadd_rn(f.x, tf.x); f.y = __fadd_rn(f.y, tf.y); f.z = __fadd_rn(f.z, tf.z);
+    };
+    if (sc.tg_nx == 0) {
+        for (uint32_t t = 0; t < sc.t; ++t) add(sc.t_off + t);
+        return;
+    }
+    const float cx = floorf(__fmul_rn(__fsub_rn(p.x, sc.tg_ox), sc.tg_inv));
+    const float cy = floorf(__fmul_rn(__fsub_rn(p.y, sc.tg_oy), sc.tg_inv));
+    const float cz = floorf(__fmul_rn(__fsub_rn(p.z, sc.tg_oz), sc.tg_inv));
+    if (!(cx >= 0.f && cx < (float)sc.tg_nx && cy >= 0.f && cy < (float)sc.tg_ny && cz >= 0.f &&
+          cz < (float)sc.tg_nz))
+        return;
+    const uint32_t c = sc.tg_cell_off + ((uint32_t)cz * sc.tg_ny + (uint32_t)cy) * sc.tg_nx + (uint32_t)cx;
+    const uint32_t end = __ldg(tm.cells + c + 1);
+    for (uint32_t k = __ldg(tm.cells + c); k < end; ++k) add(__ldg(tm.list + k));
+}
+
 template <bool kRecordAccel, bool kExact>
 __device__ __forceinline__ uint32_t integrate_particle(const SceneDesc& sc, uint32_t i, const float4& p, const float4& v,
-                                                       float rho, const PairSums& s, const float* __restrict__ tris,
+                                                       float rho, const PairSums& s, const TriangleMesh& tm,
                                                        float4* __restrict__ pos_out, float4* __restrict__ vel_out,
                                                        uint32_t* __restrict__ key_out, float4* accel)
 {
@@ -854,10 +891,7 @@ __device__ __forceinline__ uint32_t integrate_particle(const SceneDesc& sc, uint
     f.x = __fadd_rn(__fadd_rn(f.x, __fmul_rn(s.fv.x, s2)), __fmul_rn(s.fs.x, s1));
     f.y = __fadd_rn(__fadd_rn(f.y, __fmul_rn(s.fv.y, s2)), __fmul_rn(s.fs.y, s1));
     f.z = __fadd_rn(__fadd_rn(f.z, __fmul_rn(s.fv.z, s2)), __fmul_rn(s.fs.z, s1));
-    for (uint32_t t = 0; t < sc.t; ++t) {
-        const float3 tf = triangle_force(make_float3(p.x, p.y, p.z), tris + 9u * (sc.t_off + t));
-        f.x = __fadd_rn(f.x, tf.x); f.y = __fadd_rn(f.y, tf.y); f.z = __fadd_rn(f.z, tf.z);
-    }
+    add_triangle_forces(sc, tm, make_float3(p.x, p.y, p.z), f);
     float3 acc;
     acc.x = __fadd_rn(__fdiv_rn(f.x, rho), sc.gx);
     acc.y = __fadd_rn(__fdiv_rn(f.y, rho), sc.gy);
@@ -890,7 +924,7 @@ struct ForceOut {
 template <bool kRecordAccel, bool kExact>
 __device__ __forceinline__ void force_tile(const Tile& tile, const SceneDesc* scenes, const float4* __restrict__ pos,
                                            const float4* __restrict__ vel, const uint32_t* __restrict__ tag,
-                                           const StaticTables& st, const float* __restrict__ tris, const NbrArgs& nl,
+                                           const StaticTables& st, const TriangleMesh& tm, const NbrArgs& nl,
                                            const ForceOut& o)
 {
     const SceneDesc& sc = scenes[tile.scene];
@@ -932,7 +966,7 @@ __device__ __forceinline__ void force_tile(const Tile& tile, const SceneDesc* sc
             lp = nl.snbr + i;
             for (uint32_t k = 0; k < cs; ++k, lp += stride)
                 add_static_pair<kExact>(s, p, api, h, static_entry_pos(__ldg(lp), st), tag, i);
-            g = sc.q_off + integrate_particle<kRecordAccel, kExact>(sc, i, p, v, rho, s, tris, o.pos_out, o.vel_out,
+            g = sc.q_off + integrate_particle<kRecordAccel, kExact>(sc, i, p, v, rho, s, tm, o.pos_out, o.vel_out,
                                                                     o.key_out, o.accel);
         }
     }
@@ -945,7 +979,7 @@ template <bool kRecordAccel, bool kExact>
 __device__ __forceinline__ void force_overflow_tile(const Tile& tile, const SceneDesc* scenes,
                                                     const float4* __restrict__ pos, const float4* __restrict__ vel,
                                                     const uint32_t* __restrict__ tag, const uint32_t* __restrict__ start,
-                                                    const StaticTables& st, const float* __restrict__ tris,
+                                                    const StaticTables& st, const TriangleMesh& tm,
                                                     const NbrArgs& nl, const ForceOut& o)
 {
     const SceneDesc& sc = scenes[tile.scene];
@@ -970,7 +1004,7 @@ __device__ __forceinline__ void force_overflow_tile(const Tile& tile, const Scen
             sc, i, p, w, pos, start, st,
             [&](uint32_t j, const float4& q, float) { add_dynamic_pair<kExact>(s, p, v, pi, h, q, __ldg(vel + j), tag, i); },
             [&](uint32_t, const float4& q, float) { add_static_pair<kExact>(s, p, api, h, q, tag, i); });
-        g = sc.q_off + integrate_particle<kRecordAccel, kExact>(sc, i, p, v, rho, s, tris, o.pos_out, o.vel_out,
+        g = sc.q_off + integrate_particle<kRecordAccel, kExact>(sc, i, p, v, rho, s, tm, o.pos_out, o.vel_out,
                                                                 o.key_out, o.accel);
     }
     const uint32_t r = warp_aggregated_increment(o.count, g, valid);

@@ -155,6 +155,8 @@ public:
     uint32_t* sbitmap = nullptr;   // static-presence bitmaps (words)
     SceneDesc* d_sfscenes = nullptr;
     float* tris = nullptr;
+    uint32_t* tri_cells = nullptr;  // triangle cells of every scene with triangles
+    uint32_t* tri_list = nullptr;
     float4* accel = nullptr;       // recorded acceleration per sorted slot
     float4* accel_tmp = nullptr;   // as the force pass writes it (per tmp slot)
     float4* accel_io = nullptr;

@@ -56,6 +56,11 @@ __device__ __forceinline__ StaticTables static_tables(const StepArgs& a)
     return StaticTables{a.spos, a.sstart, a.spos_ref, a.sstart_ref, a.sbitmap};
 }
 
+__device__ __forceinline__ TriangleMesh triangle_mesh(const StepArgs& a)
+{
+    return TriangleMesh{a.tris, a.tri_cells, a.tri_list};
+}
+
 __device__ __forceinline__ ForceOut force_out(const StepArgs& a)
 {
     return ForceOut{a.pos_tmp, a.vel_tmp, a.key, a.arrival, a.count, a.accel};
@@ -71,7 +76,7 @@ __global__ void __launch_bounds__(kDensityThreads, SPH_DENSITY_MIN_CTAS) k_densi
 template <bool kRecord, bool kExact>
 __global__ void __launch_bounds__(kTileThreads, SPH_FORCE_MIN_CTAS) k_force(StepArgs a)
 {
-    force_tile<kRecord, kExact>(a.tiles[blockIdx.x], a.scenes, a.pos, a.vel, a.tag, static_tables(a), a.tris,
+    force_tile<kRecord, kExact>(a.tiles[blockIdx.x], a.scenes, a.pos, a.vel, a.tag, static_tables(a), triangle_mesh(a),
                                 nbr_args(a), force_out(a));
 }
 
@@ -82,7 +87,7 @@ __global__ void __launch_bounds__(kTileThreads) k_force_overflow(StepArgs a)
 {
     if (a.tile_overflow[blockIdx.x] == 0u) return;
     force_overflow_tile<kRecord, kExact>(a.tiles[blockIdx.x], a.scenes, a.pos, a.vel, a.tag, a.start,
-                                         static_tables(a), a.tris, nbr_args(a), force_out(a));
+                                         static_tables(a), triangle_mesh(a), nbr_args(a), force_out(a));
     __syncthreads();
     if (threadIdx.x == 0) a.tile_overflow[blockIdx.x] = 0u;   // every thread has read the flag
 }
@@ -127,13 +132,14 @@ __global__ void __launch_bounds__(kTileThreads) k_step_persistent(StepArgs a, ui
     const NbrArgs nl = nbr_args(a);
     const StaticTables st = static_tables(a);
     const ForceOut fo = force_out(a);
+    const TriangleMesh tm = triangle_mesh(a);
     for (uint32_t t = blockIdx.x; t < a.num_tiles; t += gridDim.x)
         density_tile<kExact>(t, a.tiles[t], threadIdx.x, a.scenes, a.pos, a.vel, a.start, st, nl);
     grid_barrier(a.bar_count, a.bar_gen, a.err);
     for (uint32_t t = blockIdx.x; t < a.num_tiles; t += gridDim.x) {
-        force_tile<false, kExact>(a.tiles[t], a.scenes, a.pos, a.vel, a.tag, st, a.tris, nl, fo);
+        force_tile<false, kExact>(a.tiles[t], a.scenes, a.pos, a.vel, a.tag, st, tm, nl, fo);
         if (a.tile_overflow[t]) {
-            force_overflow_tile<false, kExact>(a.tiles[t], a.scenes, a.pos, a.vel, a.tag, a.start, st, a.tris, nl, fo);
+            force_overflow_tile<false, kExact>(a.tiles[t], a.scenes, a.pos, a.vel, a.tag, a.start, st, tm, nl, fo);
             __syncthreads();
             if (threadIdx.x == 0) a.tile_overflow[t] = 0u;
         }
@@ -235,13 +241,14 @@ void StepState::release()
     void* ptrs[] = {d_scenes, d_sscenes, d_sfscenes, d_tiles, d_stiles, pos, vel, pos_tmp, vel_tmp, key, arrival,
                     ptag, count, start, scan_status, scan_ticket, err, bar, spos, sstart, spos_ref, sstart_ref, tris,
                     accel, accel_tmp, accel_io, staging, d_tmp_tiles_, d_tmp_scene_, nbr, snbr, ncount, tile_overflow,
-                    saved_pos_, saved_vel_, saved_start_, sbitmap, tag, tag_io, saved_tag_};
+                    saved_pos_, saved_vel_, saved_start_, sbitmap, tag, tag_io, saved_tag_, tri_cells, tri_list};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     d_scenes = d_sscenes = d_sfscenes = d_tmp_scene_ = nullptr;
     saved_pos_ = saved_vel_ = nullptr;
     saved_start_ = nullptr;
     tag = tag_io = saved_tag_ = nullptr;
+    tri_cells = tri_list = nullptr;
     grid_cache_ = 0;
     spos_ref = nullptr;
     sstart_ref = nbr = snbr = ncount = tile_overflow = sbitmap = nullptr;
@@ -294,6 +301,91 @@ SceneDesc scene_desc_for(const SceneInput& in)
     d.fm_sf = make_fastmod(d.sf_buckets);
     d.sbm_mask = in.s ? static_bitmap_bits(in.s) - 1u : 0u;
     return d;
+}
+
+// ---- triangle cells ---------------------------------------------------------
+//
+// A uniform grid over the triangles' box grown by the reach; each cell lists,
+// in increasing index, every triangle whose box grown by the reach (plus a
+// margin for the rounding of the distance) reaches into the cell.  A point's
+// cell is floor((p - o) * inv) in float, computed identically here and on the
+// device; that is monotone in p, so every point within reach of a triangle
+// lands in a cell that lists it.  Cells are half the reach wide, at most 96
+// per axis; a grid that would list more than 2^26 entries is coarsened.
+static float cell_of(float x, float o, float inv)
+{
+    volatile float d = x - o;   // rounded as on the device: no contraction
+    volatile float m = d * inv;
+    return std::floor((float)m);
+}
+
+static bool build_triangle_cells(const float* tris, uint32_t t, uint32_t t_off, SceneDesc& d,
+                                 std::vector<uint32_t>& cells, std::vector<uint32_t>& list)
+{
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    float mag = 0.f;
+    for (size_t k = 0; k < 9ull * t; ++k) {
+        const float v = tris[k];
+        if (!std::isfinite(v)) return false;   // no cells: every triangle for every particle
+        lo[k % 3] = std::min(lo[k % 3], v);
+        hi[k % 3] = std::max(hi[k % 3], v);
+        mag = std::max(mag, std::fabs(v));
+    }
+    const float reach = kTriangleReach + 1e-4f * (kTriangleReach + mag) + 1e-6f;
+    float o[3], ext = 0.f;
+    for (int a = 0; a < 3; ++a) {
+        o[a] = lo[a] - reach;
+        ext = std::max(ext, (hi[a] + reach) - o[a]);
+    }
+    for (float cs = std::max(0.5f * kTriangleReach, ext / 96.f);; cs *= 1.5f) {
+        const float inv = 1.0f / cs;
+        uint32_t n[3];
+        for (int a = 0; a < 3; ++a) n[a] = (uint32_t)cell_of(hi[a] + reach, o[a], inv) + 1u;
+        const uint64_t ncell = (uint64_t)n[0] * n[1] * n[2];
+        // per triangle: its cell range on each axis
+        std::vector<uint32_t> r(6ull * t);
+        uint64_t total = 0;
+        for (uint32_t k = 0; k < t; ++k) {
+            const float* v = tris + 9ull * k;
+            uint64_t cnt = 1;
+            for (int a = 0; a < 3; ++a) {
+                const float tlo = std::min(std::min(v[a], v[3 + a]), v[6 + a]);
+                const float thi = std::max(std::max(v[a], v[3 + a]), v[6 + a]);
+                const float c0 = std::max(cell_of(tlo - reach, o[a], inv), 0.f);
+                const float c1 = std::min(cell_of(thi + reach, o[a], inv), (float)(n[a] - 1));
+                r[6ull * k + 2 * a] = (uint32_t)c0;
+                r[6ull * k + 2 * a + 1] = (uint32_t)c1;
+                cnt *= (uint64_t)(c1 - c0 + 1.f);
+            }
+            total += cnt;
+        }
+        if (total > (1ull << 26) && ncell > 1) continue;
+        const uint32_t base = (uint32_t)cells.size();
+        std::vector<uint32_t> count(ncell + 1, 0);
+        auto each_cell = [&](uint32_t k, auto&& fn) {
+            const uint32_t* q = &r[6ull * k];
+            for (uint32_t z = q[4]; z <= q[5]; ++z)
+                for (uint32_t y = q[2]; y <= q[3]; ++y)
+                    for (uint32_t x = q[0]; x <= q[1]; ++x) fn(((uint64_t)z * n[1] + y) * n[0] + x);
+        };
+        for (uint32_t k = 0; k < t; ++k) each_cell(k, [&](uint64_t c) { ++count[c + 1]; });
+        for (uint64_t c = 0; c < ncell; ++c) count[c + 1] += count[c];
+        const uint32_t lbase = (uint32_t)list.size();
+        list.resize(list.size() + total);
+        std::vector<uint32_t> fill(count.begin(), count.end() - 1);
+        for (uint32_t k = 0; k < t; ++k)   // increasing k: each cell's list stays in triangle order
+            each_cell(k, [&](uint64_t c) { list[lbase + fill[c]++] = t_off + k; });
+        for (uint64_t c = 0; c <= ncell; ++c) cells.push_back(lbase + count[c]);
+        d.tg_ox = o[0];
+        d.tg_oy = o[1];
+        d.tg_oz = o[2];
+        d.tg_inv = inv;
+        d.tg_nx = n[0];
+        d.tg_ny = n[1];
+        d.tg_nz = n[2];
+        d.tg_cell_off = base;
+        return true;
+    }
 }
 
 // The same scene with a static index space in the dynamic fields, so the
@@ -456,6 +548,9 @@ sph_status StepState::build(int device, cudaStream_t stream, const std::vector<S
     total_n = (uint32_t)p_off;
     total_s = (uint32_t)s_off;
     total_t = (uint32_t)t_off;
+    std::vector<uint32_t> tcells, tlist;
+    for (size_t k = 0; k < inputs.size(); ++k)
+        if (inputs[k].t) build_triangle_cells(inputs[k].tris, inputs[k].t, scenes[k].t_off, scenes[k], tcells, tlist);
     scan_len = (uint32_t)q_off + 1u;
     sscan_len = (uint32_t)sq_off + 1u;
     sfscan_len = (uint32_t)sf_off + 1u;
@@ -463,6 +558,13 @@ sph_status StepState::build(int device, cudaStream_t stream, const std::vector<S
                                  (uint32_t)sbm_off, total_t, (uint32_t)scenes.size(),
                                  (uint32_t)std::max(tiles.size(), stiles.size()));
     if (st != SPH_OK) return st;
+    if (!tcells.empty()) {
+        if ((st = dev_alloc(&tri_cells, tcells.size())) != SPH_OK) return st;
+        if ((st = dev_alloc(&tri_list, std::max<size_t>(tlist.size(), 1))) != SPH_OK) return st;
+        CUDA_TRY(cudaMemcpyAsync(tri_cells, tcells.data(), sizeof(uint32_t) * tcells.size(), cudaMemcpyHostToDevice, stream_));
+        if (!tlist.empty())
+            CUDA_TRY(cudaMemcpyAsync(tri_list, tlist.data(), sizeof(uint32_t) * tlist.size(), cudaMemcpyHostToDevice, stream_));
+    }
     std::vector<SceneDesc> sview, sfview;
     for (const auto& d : scenes) {
         sview.push_back(static_view(d, false));
@@ -775,6 +877,8 @@ StepArgs StepState::step_args() const
     a.spos_ref = spos_ref;
     a.sstart_ref = sstart_ref;
     a.tris = tris;
+    a.tri_cells = tri_cells;
+    a.tri_list = tri_list;
     a.sbitmap = sbitmap;
     a.accel = accel_tmp;
     a.err = err;

@@ -159,5 +159,38 @@ def test_exact_scene_file_with_boundary_mesh(tmp_path):
     path = tmp_path / "scene.json"
     path.write_text(json.dumps(doc))
     sc = scene_json.load_scene(str(path), dt=1e-4)
-    assert sc.triangles.shape == (3, 9) and sc.n > 5000
+    assert sc.triangles.shape == (3, 9) and sc.n == 12 * 10 * 12
     run_against_oracle(sc, [1, 4, 10])
+
+
+def uv_sphere(radius, centre, rings, segments):
+    """Triangles (T, 9) of a UV sphere: two per quad, one per pole quad."""
+    c = np.asarray(centre, np.float64)
+    th = np.linspace(0.0, np.pi, rings + 1)
+    ph = np.linspace(0.0, 2.0 * np.pi, segments + 1)
+    P = lambda i, j: c + radius * np.array([np.sin(th[i]) * np.cos(ph[j]), np.cos(th[i]),  # noqa: E731
+                                             np.sin(th[i]) * np.sin(ph[j])])
+    tris = []
+    for i in range(rings):
+        for j in range(segments):
+            a, b, cc, d = P(i, j), P(i + 1, j), P(i + 1, j + 1), P(i, j + 1)
+            if i > 0:
+                tris.append(np.concatenate([a, b, d]))
+            if i < rings - 1:
+                tris.append(np.concatenate([b, cc, d]))
+    return np.asarray(tris, np.float32)
+
+
+def test_exact_triangle_cells_large_mesh():
+    """A mesh much larger than the triangle reach (2.5): each particle
+    evaluates only the triangles of its cell, and the result still equals
+    the oracle, which evaluates all of them; particles lie at every distance
+    from the sphere, many near the reach."""
+    h = 2.0
+    dyn = scenes.filled_box((16, 16, 16), 0.5, (-4.0, -1.0, -4.0), 0.0, None)
+    params = scenes.Params(particle_mass=1.0, gas_constant=200.0, elasticity=1.0, viscosity=0.1,
+                           gravity=(0.0, -9.81, 0.0), rest_density=1.0, h=h)
+    sc = scenes.Scene(name="sphere_mesh", dyn_pos=dyn, static_pos=np.zeros((0, 3), np.float32), params=params,
+                      dt=1e-3, steps=0, triangles=uv_sphere(7.0, (0.0, 3.0, 0.0), 18, 32))
+    assert sc.triangles.shape[0] > 500
+    run_against_oracle(sc, [1, 2])
