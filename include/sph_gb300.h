@@ -181,6 +181,36 @@ SPH_API sph_status sph_engine_kernel_times(sph_engine* engine, float* ms, int co
  * own work or timing events with the engine's launches. */
 SPH_API sph_status sph_engine_get_stream(sph_engine* engine, void** stream);
 
+/* ---- headless particle rendering ----------------------------------------
+ * The reference's particle renderer (ParticleRenderer.cpp:75-82 with
+ * Shaders/particle.vert:67-117 and particle.frag:17-22) without a graphics
+ * stack: each particle is a camera-facing quad of half-size `size` around its
+ * view-space centre, cut to the disc inside it; colour mix(color, red,
+ * clamp(1 - exp(-pressure/2000), 0, 1)) with alpha faded out within 4-5
+ * units of the eye; depth test LESS, first drawn wins ties, drawn in the
+ * reference's order (dynamic particles by buffer index, then statics). */
+typedef struct sph_render_view {
+    float proj[16];      /* u_projMatrix, column-major (element [col*4 + row]) */
+    float view[16];      /* u_viewMatrix */
+    float model[16];     /* u_modelMatrix */
+    uint32_t width, height;
+} sph_render_view;
+
+typedef struct sph_render_layer {
+    float size;          /* u_size */
+    float color[4];      /* u_color, RGBA in [0, 1] */
+} sph_render_layer;
+
+/* Renders scene state into host images: rgba (width*height*4 bytes, RGBA8,
+ * row 0 at the bottom as in GL window coordinates) and depth (width*height
+ * floats, window depth in [0, 1], 1 where nothing was drawn); either may be
+ * NULL.  A NULL layer is not drawn.  The reference's application draws the
+ * dynamic layer at size 0.1 and the static one at 0.03
+ * (SimulationVisualisationScene.cpp:60-61). */
+SPH_API sph_status sph_engine_render(sph_engine* engine, const sph_render_view* view,
+                                     const sph_render_layer* dynamic_layer, const sph_render_layer* static_layer,
+                                     uint8_t* rgba, float* depth);
+
 /* ---- the counting sort stage on its own ---------------------------------
  * Hash + count + scan + scatter of n positions into `buckets` buckets with
  * cell size h, on the device (SF:321-356 with the serial scan of

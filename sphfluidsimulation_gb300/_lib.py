@@ -29,6 +29,15 @@ class SphParams(C.Structure):
                 ("gravity_z", C.c_float), ("rest_density", C.c_float), ("max_interaction_distance", C.c_float)]
 
 
+class SphRenderView(C.Structure):
+    _fields_ = [("proj", C.c_float * 16), ("view", C.c_float * 16), ("model", C.c_float * 16),
+                ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
+class SphRenderLayer(C.Structure):
+    _fields_ = [("size", C.c_float), ("color", C.c_float * 4)]
+
+
 STATUS = {0: "SPH_OK", 1: "SPH_ERR_INVALID_ARGUMENT", 2: "SPH_ERR_NOT_INITIALIZED", 3: "SPH_ERR_CUDA",
           4: "SPH_ERR_OUT_OF_MEMORY", 5: "SPH_ERR_DEVICE_TIMEOUT", 6: "SPH_ERR_CAPACITY", 7: "SPH_ERR_BUDGET",
           8: "SPH_ERR_NOT_FOUND"}
@@ -61,6 +70,8 @@ _SIGS = {
     "sph_engine_count": (_st, [_vp, C.c_int, _u64p]),
     "sph_engine_record_acceleration": (_st, [_vp, C.c_int]),
     "sph_engine_set_exact": (_st, [_vp, C.c_int]),
+    "sph_engine_render": (_st, [_vp, C.POINTER(SphRenderView), C.POINTER(SphRenderLayer), C.POINTER(SphRenderLayer),
+                                _vp, _fp]),
     "sph_engine_read_acceleration": (_st, [_vp, _fp]),
     "sph_engine_set_timing": (_st, [_vp, C.c_int]),
     "sph_engine_kernel_times": (_st, [_vp, _fp, C.c_int]),

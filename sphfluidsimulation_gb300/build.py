@@ -23,7 +23,9 @@ OUT_DIR = os.path.join(PKG, "_lib")
 BUILD_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT_DIR, "libsph_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
+# host code is compiled without floating-point contraction, so host-side
+# float arithmetic (render matrices, triangle cells) rounds every operation
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden,-ffp-contract=off",
                      "-I", INCLUDE, "-I", CSRC]
 
 

@@ -257,6 +257,16 @@ SPH_API sph_status sph_engine_count(sph_engine* e, int which, uint64_t* value)
     return SPH_OK;
 }
 
+SPH_API sph_status sph_engine_render(sph_engine* e, const sph_render_view* view,
+                                     const sph_render_layer* dynamic_layer, const sph_render_layer* static_layer,
+                                     uint8_t* rgba, float* depth)
+{
+    if (!e || !view) return SPH_ERR_INVALID_ARGUMENT;
+    if (!e->initialized) return SPH_ERR_NOT_INITIALIZED;
+    API_CUDA_TRY(cudaSetDevice(e->device));
+    return e->state.render(*view, dynamic_layer, static_layer, rgba, depth);
+}
+
 SPH_API sph_status sph_engine_set_exact(sph_engine* e, int exact)
 {
     if (!e) return SPH_ERR_INVALID_ARGUMENT;

@@ -51,6 +51,25 @@ enum class StepMode { Staged = 0, Persistent = 1 };
 
 void set_last_error(const std::string& s);
 const char* last_error();
+
+#define CUDA_TRY(expr)                                                                              \
+    do {                                                                                            \
+        cudaError_t e_ = (expr);                                                                    \
+        if (e_ != cudaSuccess) {                                                                    \
+            set_last_error(std::string(#expr) + ": " + cudaGetErrorString(e_));                    \
+            return e_ == cudaErrorMemoryAllocation ? SPH_ERR_OUT_OF_MEMORY : SPH_ERR_CUDA;          \
+        }                                                                                           \
+    } while (0)
+
+template <typename T>
+inline sph_status dev_alloc(T** p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0) count = 1;
+    CUDA_TRY(cudaMalloc((void**)p, sizeof(T) * count));
+    return SPH_OK;
+}
+
 sph_status validate_scene(const SceneInput& in);
 // Physics constants and sizes of a scene (offsets left zero).
 SceneDesc scene_desc_for(const SceneInput& in);
@@ -111,6 +130,10 @@ public:
     uint32_t cap_sq() const { return cap_sq_; }
     uint32_t cap_sf() const { return cap_sf_; }
     uint32_t cap_sbm() const { return cap_sbm_; }
+
+    // Headless particle splats of scene 0 (see sph_engine_render).
+    sph_status render(const sph_render_view& view, const sph_render_layer* dyn, const sph_render_layer* stat,
+                      uint8_t* rgba_out, float* depth_out);
 
     // Copies the state a step reads (sorted particles and the bucket table)
     // aside and back, so trial steps leave the simulation where it was.
@@ -194,6 +217,10 @@ private:
     float4* saved_vel_ = nullptr;
     uint32_t* saved_start_ = nullptr;
     uint32_t* saved_tag_ = nullptr;
+    unsigned long long* render_zkey_ = nullptr;   // render targets, kept between frames
+    uchar4* render_rgba_ = nullptr;
+    float* render_depth_ = nullptr;
+    size_t render_pixels_ = 0;
     SceneDesc* d_tmp_scene_ = nullptr;     // its dynamic and two static views
 };
 

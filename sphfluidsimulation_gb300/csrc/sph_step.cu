@@ -215,24 +215,6 @@ thread_local std::string g_last_error;
 void set_last_error(const std::string& s) { g_last_error = s; }
 const char* last_error() { return g_last_error.c_str(); }
 
-#define CUDA_TRY(expr)                                                                              \
-    do {                                                                                            \
-        cudaError_t e_ = (expr);                                                                    \
-        if (e_ != cudaSuccess) {                                                                    \
-            set_last_error(std::string(#expr) + ": " + cudaGetErrorString(e_));                    \
-            return e_ == cudaErrorMemoryAllocation ? SPH_ERR_OUT_OF_MEMORY : SPH_ERR_CUDA;          \
-        }                                                                                           \
-    } while (0)
-
-template <typename T>
-static sph_status dev_alloc(T** p, size_t count)
-{
-    *p = nullptr;
-    if (count == 0) count = 1;
-    CUDA_TRY(cudaMalloc((void**)p, sizeof(T) * count));
-    return SPH_OK;
-}
-
 StepState::~StepState() { release(); }
 
 void StepState::release()
@@ -241,7 +223,8 @@ void StepState::release()
     void* ptrs[] = {d_scenes, d_sscenes, d_sfscenes, d_tiles, d_stiles, pos, vel, pos_tmp, vel_tmp, key, arrival,
                     ptag, count, start, scan_status, scan_ticket, err, bar, spos, sstart, spos_ref, sstart_ref, tris,
                     accel, accel_tmp, accel_io, staging, d_tmp_tiles_, d_tmp_scene_, nbr, snbr, ncount, tile_overflow,
-                    saved_pos_, saved_vel_, saved_start_, sbitmap, tag, tag_io, saved_tag_, tri_cells, tri_list};
+                    saved_pos_, saved_vel_, saved_start_, sbitmap, tag, tag_io, saved_tag_, tri_cells, tri_list,
+                    render_zkey_, render_rgba_, render_depth_};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     d_scenes = d_sscenes = d_sfscenes = d_tmp_scene_ = nullptr;
@@ -249,6 +232,10 @@ void StepState::release()
     saved_start_ = nullptr;
     tag = tag_io = saved_tag_ = nullptr;
     tri_cells = tri_list = nullptr;
+    render_zkey_ = nullptr;
+    render_rgba_ = nullptr;
+    render_depth_ = nullptr;
+    render_pixels_ = 0;
     grid_cache_ = 0;
     spos_ref = nullptr;
     sstart_ref = nbr = snbr = ncount = tile_overflow = sbitmap = nullptr;

@@ -149,6 +149,32 @@ class SimulationEngineCUDA:
         bit-identical to its synchronous CPU engine) or the fast fused form."""
         check(self.lib.sph_engine_set_exact(self.h, int(exact)), "sph_engine_set_exact")
 
+    def render(self, proj, view, model, width: int, height: int, dynamic_layer=(0.1, (1.0, 1.0, 1.0, 1.0)),
+               static_layer=(0.03, (0.0, 0.0, 1.0, 1.0))):
+        """Headless particle splats (sph_engine_render): (rgba (height, width,
+        4) uint8 with row 0 at the bottom, depth (height, width) float32).
+        Matrices are column-major 4x4 (sphfluidsimulation_gb300.render); a
+        layer is (size, rgba) or None."""
+        v = _lib.SphRenderView()
+        for name, m in (("proj", proj), ("view", view), ("model", model)):
+            arr = np.ascontiguousarray(np.asarray(m, np.float32).reshape(16))
+            getattr(v, name)[:] = arr.tolist()
+        v.width, v.height = int(width), int(height)
+
+        def layer(l):
+            if l is None:
+                return None
+            out = _lib.SphRenderLayer()
+            out.size = float(l[0])
+            out.color[:] = [float(c) for c in l[1]]
+            return C.byref(out)
+
+        rgba = np.empty((height, width, 4), np.uint8)
+        depth = np.empty((height, width), np.float32)
+        check(self.lib.sph_engine_render(self.h, C.byref(v), layer(dynamic_layer), layer(static_layer),
+                                         rgba.ctypes.data_as(C.c_void_p), _fptr(depth)), "sph_engine_render")
+        return rgba, depth
+
     def record_acceleration(self, on: bool = True) -> None:
         check(self.lib.sph_engine_record_acceleration(self.h, int(on)), "sph_engine_record_acceleration")
 

@@ -65,6 +65,10 @@ def _load(path: str):
     lib.sph_oracle_derived.argtypes = [_vp, _dp, _dp]
     lib.sph_oracle_hash.argtypes = [_fp, C.c_uint32, C.c_float, C.c_uint32, _up]
     lib.sph_oracle_counting_sort.argtypes = [_up, C.c_uint32, C.c_uint32, _up, _up, _up]
+    if hasattr(lib, "sph_oracle_splat"):
+        lib.sph_oracle_splat.restype = C.c_int
+        lib.sph_oracle_splat.argtypes = [_fp, _fp, _fp, C.c_uint32, C.c_uint32, _fp, C.c_uint32, C.c_float, _fp,
+                                         _fp, C.c_uint32, C.c_float, _fp, _vp, _vp, _fp]
     return lib
 
 
@@ -253,3 +257,26 @@ class RefEngine:
         keys = np.zeros(p.shape[0], np.uint32)
         self.L.sph_ref_hash(_ptr(p, _fp), p.shape[0], float(h), int(mod), _ptr(keys, _up))
         return keys
+
+
+def oracle_splat(proj, view, model, width: int, height: int, dyn4, dyn_layer, stat3, stat_layer):
+    """The CPU restatement of sph_engine_render (oracle/sph_splat.c).  dyn4:
+    (n, 4) x, y, z, pressure in the reference's buffer order; stat3: (s, 3)
+    in its sorted static order; a layer is (size, rgba) or None.  Returns
+    (rgba (height, width, 4) uint8, depth (height, width) float32)."""
+    L = lib()
+    m = [np.ascontiguousarray(np.asarray(x, np.float32).reshape(16)) for x in (proj, view, model)]
+    d = np.ascontiguousarray(dyn4, np.float32).reshape(-1, 4)
+    st = np.ascontiguousarray(stat3, np.float32).reshape(-1, 3)
+    dc = None if dyn_layer is None else np.ascontiguousarray(dyn_layer[1], np.float32)
+    sc = None if stat_layer is None else np.ascontiguousarray(stat_layer[1], np.float32)
+    zkey = np.empty(width * height, np.uint64)
+    rgba = np.empty((height, width, 4), np.uint8)
+    depth = np.empty((height, width), np.float32)
+    rc = L.sph_oracle_splat(_ptr(m[0], _fp), _ptr(m[1], _fp), _ptr(m[2], _fp), width, height,
+                            _ptr(d, _fp), d.shape[0], 0.0 if dyn_layer is None else float(dyn_layer[0]), _ptr(dc, _fp),
+                            _ptr(st, _fp), st.shape[0], 0.0 if stat_layer is None else float(stat_layer[0]),
+                            _ptr(sc, _fp), zkey.ctypes.data, rgba.ctypes.data, _ptr(depth, _fp))
+    assert rc == 0
+    return rgba, depth
+
