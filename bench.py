@@ -270,6 +270,10 @@ def run_plain(args, world, rank, local, pg):
     e2e_s = max_over_ranks(pg, time.perf_counter() - t0, local)
     e2e_value = world * n * e2e_steps / e2e_s
 
+    render_line = None
+    if not args.no_forms and rank == 0:
+        render_line = time_render(eng, scene)
+
     line = {
         "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total_s / args.steps,
@@ -290,7 +294,35 @@ def run_plain(args, world, rank, local, pg):
         "clocks": clk,
         "wall_s_timed_region": wall,
     }
+    if render_line is not None:
+        line["render"] = render_line
     return line, scene
+
+
+def time_render(eng, scene, width: int = 1920, height: int = 1080, frames: int = 5):
+    """Headless splat frames of the current state at 1080p with the reference
+    application's layers (dynamic 0.1, static 0.03; 120 degree field of view):
+    the box scaled to 5 times its size by the model matrix and seen from 8
+    units, so it fills most of the frame.  Wall time per sph_engine_render
+    call, which includes copying the RGBA8 and depth images to the host."""
+    import math
+    from sphfluidsimulation_gb300 import render
+    lo = scene.static_pos.min(0) if scene.s else scene.dyn_pos.min(0)
+    hi = scene.static_pos.max(0) if scene.s else scene.dyn_pos.max(0)
+    centre = 5.0 * (lo + hi) / 2.0
+    eye = centre + np.array([0.0, 3.0, 7.4])
+    view = render.look_at(eye, centre)
+    proj = render.perspective(math.radians(120.0), width / height, 0.1, 1000.0)
+    model = np.diag([5.0, 5.0, 5.0, 1.0]).astype(np.float32).reshape(16)
+    rgba, _ = eng.render(proj, view, model, width, height)   # warm-up, allocates the targets
+    t0 = time.perf_counter()
+    for _ in range(frames):
+        rgba, _ = eng.render(proj, view, model, width, height)
+    ms = 1000.0 * (time.perf_counter() - t0) / frames
+    return {"width": width, "height": height, "particles": scene.n + scene.s, "frames": frames,
+            "ms_per_frame": ms, "covered_pixels": int((rgba[..., 3] > 0).sum()),
+            "d2h_bytes_per_frame": width * height * 8,
+            "camera": "box x5, eye 8 units off its centre, fov 120 deg, sizes 0.1 / 0.03"}
 
 
 def profiled_traffic(stage: str, workload: str):
