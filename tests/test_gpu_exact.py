@@ -194,3 +194,10 @@ def test_exact_triangle_cells_large_mesh():
                       dt=1e-3, steps=0, triangles=uv_sphere(7.0, (0.0, 3.0, 0.0), 18, 32))
     assert sc.triangles.shape[0] > 500
     run_against_oracle(sc, [1, 2])
+
+
+def test_exact_equals_oracle_at_one_million():
+    """The benchmark scene itself (1,048,576 particles, 256,002 walls): two
+    exact steps equal the synchronous oracle's, all bytes of every particle."""
+    sc = scenes.config1(steps=0)
+    run_against_oracle(sc, [1, 1])
