@@ -35,7 +35,7 @@ constexpr int kTileThreads = 128;          // slots per tile = threads per CTA
 #define SPH_DENSITY_MIN_CTAS 8
 #endif
 #ifndef SPH_FORCE_MIN_CTAS
-#define SPH_FORCE_MIN_CTAS 6
+#define SPH_FORCE_MIN_CTAS 7
 #endif
 #ifndef SPH_NBR_BATCH
 #define SPH_NBR_BATCH 4
