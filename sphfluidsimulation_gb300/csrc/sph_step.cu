@@ -176,15 +176,16 @@ __global__ void __launch_bounds__(kTileThreads) k_unsort(const Tile* tiles, cons
     const uint32_t i = tile.begin + threadIdx.x;
     if (i >= tile.end) return;
     const float4 p = pos[i];
-    const float4 v = vel[i];
     const uint32_t id = by_tag ? tag_in[i] : __float_as_uint(p.w);
     if (id >= sc.n) return;
-    const uint32_t key = fast_mod(cell_hash(p.x, p.y, p.z, sc.h), sc.fm_b);
     const uint32_t o = sc.p_off + id;
+    if (tag_out) tag_out[o] = tag_in[i];
+    if (!out) return;   // tags only
+    const float4 v = vel[i];
+    const uint32_t key = fast_mod(cell_hash(p.x, p.y, p.z, sc.h), sc.fm_b);
     out[2 * (size_t)o] = make_float4(p.x, p.y, p.z, v.w);
     out[2 * (size_t)o + 1] = make_float4(v.x, v.y, v.z, __uint_as_float(key));
     if (accel_in) accel_out[o] = accel_in[i];
-    if (tag_out) tag_out[o] = tag_in[i];
 }
 
 // Upload staging (caller's order, positions and velocities as float4 pairs)
@@ -1105,9 +1106,11 @@ sph_status StepState::write_scene(uint32_t scene, const sph_dynamic_particle* in
     const SceneDesc& d = scenes[scene];
     if (!d.n) return SPH_OK;
     // move the current sorted state of all scenes, and their buffer tags, into
-    // staging order first; the re-sort keeps every particle's tag
-    k_unsort<<<(unsigned)tiles.size(), kTileThreads, 0, stream_>>>(d_tiles, d_scenes, pos, vel, staging, nullptr, nullptr,
-                                                                   tag, tag_io, 0);
+    // staging order first (a lone scene is replaced whole: its tags only); the
+    // re-sort keeps every particle's tag
+    k_unsort<<<(unsigned)tiles.size(), kTileThreads, 0, stream_>>>(d_tiles, d_scenes, pos, vel,
+                                                                   scenes.size() > 1 ? staging : nullptr, nullptr,
+                                                                   nullptr, tag, tag_io, 0);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaMemcpyAsync(staging + 2ull * d.p_off, in, sizeof(sph_dynamic_particle) * d.n, cudaMemcpyHostToDevice, stream_));
     sph_status st = enqueue_load(staging, false);
