@@ -138,12 +138,8 @@ def barrier(pg):
 
 
 def max_over_ranks(pg, value: float, local: int) -> float:
-    if pg is None:
-        return value
-    import torch
-    t = torch.tensor([value], dtype=torch.float64, device=f"cuda:{local}")
-    pg.all_reduce(t, op=pg.ReduceOp.MAX)
-    return float(t.item())
+    from sphfluidsimulation_gb300 import replicas
+    return replicas.reduce_scalar(pg, value, "max")
 
 
 # ---------------------------------------------------------------------------

@@ -21,7 +21,7 @@ from typing import Dict, List
 
 import numpy as np
 
-from . import scenes
+from . import replicas, scenes
 from .engine import Batch, Server, SimulationEngineCUDA
 
 
@@ -31,8 +31,17 @@ def _percentiles(lat: List[float]) -> Dict[str, float]:
             "p99_s": float(np.percentile(a, 99)), "mean_s": float(a.mean())}
 
 
-def run_batched(steps: int, count: int = 96, seed: int = 0, mode: int = -1) -> Dict:
-    scs = scenes.batched_scenes(count=count, seed=seed, steps=steps)
+def _barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def run_batched(steps: int, count: int = 96, seed: int = 0, mode: int = -1, pg=None, world: int = 1,
+                rank: int = 0) -> Dict:
+    """With world > 1 each rank batches its share of the scenes (split by
+    footprint) and the rates are whole-job aggregates."""
+    all_scs = scenes.batched_scenes(count=count, seed=seed, steps=steps)
+    scs = replicas.rank_share(all_scs, [replicas.footprint_bytes(sc.n, sc.s) for sc in all_scs], world, rank)
     total = sum(sc.n for sc in scs)
     b = Batch()
     for sc in scs:
@@ -44,6 +53,7 @@ def run_batched(steps: int, count: int = 96, seed: int = 0, mode: int = -1) -> D
         b.set_mode(mode)
         chosen = None
     b.step(2)                                   # warm-up
+    _barrier(pg)
     t0 = time.perf_counter()
     b.step(steps)
     tb = time.perf_counter() - t0
@@ -56,15 +66,21 @@ def run_batched(steps: int, count: int = 96, seed: int = 0, mode: int = -1) -> D
         e.initialize(sc)
         e.update(sc.dt, 2)                      # warm-up, builds each step graph
         engines.append(e)
+    _barrier(pg)
     t0 = time.perf_counter()
     for e, sc in zip(engines, scs):
         e.update(sc.dt, steps)
     tp = time.perf_counter() - t0
     for e in engines:
         e.close()
-    return {"scenes": count, "particles": total, "steps": steps,
-            "batched_particle_steps_per_s": total * steps / tb, "plain_looped_particle_steps_per_s": total * steps / tp,
-            "speedup": tp / tb, "batched_ms_per_step": 1e3 * tb / steps, "plain_looped_ms_per_step": 1e3 * tp / steps,
+    batched_rate = replicas.aggregate_rate(pg, total * steps, tb)
+    plain_rate = replicas.aggregate_rate(pg, total * steps, tp)
+    tb, tp = replicas.reduce_scalar(pg, tb), replicas.reduce_scalar(pg, tp)
+    total = int(replicas.reduce_scalar(pg, total, "sum"))
+    return {"scenes": count, "particles": total, "steps": steps, "ranks": world,
+            "batched_particle_steps_per_s": batched_rate, "plain_looped_particle_steps_per_s": plain_rate,
+            "speedup": batched_rate / plain_rate, "batched_ms_per_step": 1e3 * tb / steps,
+            "plain_looped_ms_per_step": 1e3 * tp / steps,
             "persistent_grid": [grid, thr],
             "mode": ("autotuned " if chosen else "") + ("persistent" if (chosen[0] if chosen else mode) == 0 else "staged"),
             "autotune_ms_per_step": chosen[2] if chosen else None}
@@ -126,27 +142,38 @@ def _served(jobset, arrivals, budget: int, slots: int, chunk: int):
 
 
 def run_served(n_jobs: int = 200, horizon_scale: float = 0.1, seed: int = 0, budget: int = 120 << 30,
-               slots: int = 128, chunk: int = 50) -> Dict:
-    jobset = _job_set(n_jobs, horizon_scale, seed)
+               slots: int = 128, chunk: int = 50, pg=None, world: int = 1, rank: int = 0) -> Dict:
+    """With world > 1 each rank serves its share of the jobs (split by
+    footprint) on its own GPU: throughput is the whole-job aggregate and the
+    latency percentiles are over every rank's jobs."""
+    full = _job_set(n_jobs, horizon_scale, seed)
+    jobset = replicas.rank_share(full, [Server.job_bytes(sc.n, sc.s) for _, sc in full], world, rank)
+    n_jobs_all, n_jobs = n_jobs, len(jobset)
     work = sum(j.n * j.steps for j, _ in jobset)
     zeros = [0.0] * n_jobs
     # warm-up both paths on the first small job
     _fifo(jobset[:1])
     _served(jobset[:1], [0.0], budget, slots, chunk)
+    _barrier(pg)
     fifo_span, _ = _fifo(jobset)
+    _barrier(pg)
     srv_span, srv_lat_closed = _served(jobset, zeros, budget, slots, chunk)
     cap_fifo = work / fifo_span
     # Poisson arrivals at 80 % of the FIFO plain capacity
     mean_work = work / n_jobs
     rate = 0.8 * cap_fifo / mean_work
-    rng = scenes.SplitMix64(seed ^ 0xA77)
+    rng = scenes.SplitMix64((seed ^ 0xA77) + 7919 * rank)
     u = rng.uniform(n_jobs).astype(np.float64)
     arrivals = list(np.cumsum(-np.log(np.maximum(1e-12, 1.0 - u)) / rate))
     fifo_span2, fifo_lat = _fifo(jobset, arrivals)
     srv_span2, srv_lat = _served(jobset, arrivals, budget, slots, chunk)
-    return {"jobs": n_jobs, "horizon_scale": horizon_scale, "particle_steps": work,
-            "served_particle_steps_per_s": work / srv_span, "fifo_plain_particle_steps_per_s": cap_fifo,
-            "speedup": fifo_span / srv_span, "arrival_rate_per_s": rate, "load_vs_fifo_capacity": 0.8,
+    served_rate = replicas.aggregate_rate(pg, work, srv_span)
+    fifo_rate = replicas.aggregate_rate(pg, work, fifo_span)
+    srv_lat, fifo_lat = replicas.gather_values(pg, srv_lat), replicas.gather_values(pg, fifo_lat)
+    work = replicas.reduce_scalar(pg, work, "sum")
+    return {"jobs": n_jobs_all, "ranks": world, "horizon_scale": horizon_scale, "particle_steps": work,
+            "served_particle_steps_per_s": served_rate, "fifo_plain_particle_steps_per_s": fifo_rate,
+            "speedup": served_rate / fifo_rate, "arrival_rate_per_s": rate, "load_vs_fifo_capacity": 0.8,
             "served_latency": _percentiles(srv_lat), "fifo_latency": _percentiles(fifo_lat),
             "budget_bytes": budget, "slots": slots, "chunk_steps": chunk}
 
@@ -154,16 +181,16 @@ def run_served(n_jobs: int = 200, horizon_scale: float = 0.1, seed: int = 0, bud
 def run(args, world, rank, local, pg) -> Dict:
     """--workload batched|served: one JSON line in the bench contract."""
     if args.workload == "batched":
-        r = run_batched(args.steps)
+        r = run_batched(args.steps, pg=pg, world=world, rank=rank)
         return {"metric": "aggregate particle-steps/s, 96 batched dam breaks", "value": r["batched_particle_steps_per_s"],
                 "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-                "ms_per_step": r["batched_ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                "ms_per_step": r["batched_ms_per_step"], "higher_is_better": True, "scaling": "strong",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam breaks)",
                 "config": {"workload": "batched_96", "particles": r["particles"]}, "batched": r,
                 "gpu_launches": args.steps}
-    r = run_served()
+    r = run_served(pg=pg, world=world, rank=rank)
     return {"metric": "aggregate particle-steps/s, served jobs", "value": r["served_particle_steps_per_s"],
             "unit": "particle-steps/s", "n_gpus": world, "steps": None, "warmup": 1,
-            "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "ms_per_step": None, "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded dam-break jobs, Poisson arrivals)",
             "config": {"workload": "served", "jobs": r["jobs"], "horizon_scale": r["horizon_scale"]}, "served": r}
