@@ -131,12 +131,12 @@ double now_s()
 uint64_t job_bytes(uint32_t n, uint32_t s)
 {
     // per dynamic particle: sorted pos/vel 32, unsorted pos/vel 32, staging 32,
-    // key/arrival/perm 12, two buckets x (count + start) 16, neighbour lists
-    // (96 + 48 slots) 576, list counts 4;
+    // key/arrival/ptag 12, buffer tags 8, two buckets x (count + start) 16,
+    // neighbour lists (96 + 48 slots) 576, list counts 4;
     // per static particle: two sorted copies 32, staging 32, bucket count +
     // start for both tables 8 + 8 x 8 = 72
     // plus 8 bytes per static particle of static-presence bitmap
-    return 704ull * n + 144ull * s + 4096ull;
+    return 712ull * n + 144ull * s + 4096ull;
 }
 
 struct sph_server {

@@ -89,7 +89,7 @@ def rank_share(items: Sequence, footprints: Sequence[int], world: int, rank: int
 def footprint_bytes(n: int, s: int, job_bytes: Optional[callable] = None) -> int:
     """Resident bytes of a scene of n dynamic and s static particles (the
     server's estimate when given, else the dominant arrays: state, sort and
-    neighbour lists, about 700 B per particle)."""
+    neighbour lists, about 710 B per particle)."""
     if job_bytes is not None:
         return int(job_bytes(n, s))
-    return 704 * int(n) + 144 * int(s) + 4096
+    return 712 * int(n) + 144 * int(s) + 4096
