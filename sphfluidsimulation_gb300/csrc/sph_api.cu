@@ -187,8 +187,7 @@ SPH_API sph_status sph_engine_synchronize(sph_engine* e)
 {
     if (!e) return SPH_ERR_INVALID_ARGUMENT;
     API_CUDA_TRY(cudaSetDevice(e->device));
-    API_CUDA_TRY(cudaStreamSynchronize(e->stream));
-    return e->state.check_device_error();
+    return e->state.check_device_error();   // waits for the stream
 }
 
 SPH_API sph_status sph_engine_update(sph_engine* e, float dt, uint32_t steps)
@@ -482,8 +481,7 @@ SPH_API sph_status sph_batch_step(sph_batch* b, uint32_t steps)
     if (!b->finalized) API_TRY(sph_batch_finalize(b));
     API_CUDA_TRY(cudaSetDevice(b->device));
     API_TRY(b->state.enqueue_steps(steps, b->mode, false, false));
-    API_CUDA_TRY(cudaStreamSynchronize(b->stream));
-    return b->state.check_device_error();
+    return b->state.check_device_error();   // waits for the stream
 }
 
 SPH_API sph_status sph_batch_read_scene(sph_batch* b, uint32_t scene_id, sph_dynamic_particle* out)

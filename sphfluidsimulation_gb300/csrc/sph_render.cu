@@ -314,7 +314,6 @@ sph_status StepState::render(const sph_render_view& view, const sph_render_layer
         CUDA_TRY(cudaMemcpyAsync(rgba_out, render_rgba_, 4 * pixels, cudaMemcpyDeviceToHost, stream_));
     if (depth_out)
         CUDA_TRY(cudaMemcpyAsync(depth_out, render_depth_, sizeof(float) * pixels, cudaMemcpyDeviceToHost, stream_));
-    CUDA_TRY(cudaStreamSynchronize(stream_));
     return check_device_error();
 }
 

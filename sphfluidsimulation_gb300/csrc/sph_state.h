@@ -217,6 +217,7 @@ private:
     float4* saved_vel_ = nullptr;
     uint32_t* saved_start_ = nullptr;
     uint32_t* saved_tag_ = nullptr;
+    uint32_t* err_host_ = nullptr;                // pinned copy of the status word
     unsigned long long* render_zkey_ = nullptr;   // render targets, kept between frames
     uchar4* render_rgba_ = nullptr;
     float* render_depth_ = nullptr;

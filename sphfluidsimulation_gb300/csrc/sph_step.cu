@@ -229,6 +229,7 @@ void StepState::release()
     for (void* p : ptrs)
         if (p) cudaFree(p);
     d_scenes = d_sscenes = d_sfscenes = d_tmp_scene_ = nullptr;
+    if (err_host_) { cudaFreeHost(err_host_); err_host_ = nullptr; }
     saved_pos_ = saved_vel_ = nullptr;
     saved_start_ = nullptr;
     tag = tag_io = saved_tag_ = nullptr;
@@ -590,7 +591,6 @@ sph_status StepState::build(int device, cudaStream_t stream, const std::vector<S
         if ((st = enqueue_load(staging, false)) != SPH_OK) return st;
         if ((st = enqueue_sort(0)) != SPH_OK) return st;
     }
-    CUDA_TRY(cudaStreamSynchronize(stream_));
     return check_device_error();
 }
 
@@ -1026,12 +1026,18 @@ sph_status StepState::enqueue_steps(uint32_t steps, StepMode mode, bool record_a
     return SPH_OK;
 }
 
+// Waits for the stream and reads the device status word with one round trip:
+// the word is copied into pinned host memory behind the queued work.
 sph_status StepState::check_device_error()
 {
-    if (!err) return SPH_OK;
-    uint32_t h = 0;
-    CUDA_TRY(cudaMemcpyAsync(&h, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
+    if (!err) {
+        CUDA_TRY(cudaStreamSynchronize(stream_));
+        return SPH_OK;
+    }
+    if (!err_host_) CUDA_TRY(cudaMallocHost((void**)&err_host_, sizeof(uint32_t)));
+    CUDA_TRY(cudaMemcpyAsync(err_host_, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
     CUDA_TRY(cudaStreamSynchronize(stream_));
+    const uint32_t h = *err_host_;
     if (h) {
         CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(uint32_t), stream_));
         CUDA_TRY(cudaMemsetAsync(bar, 0, 2 * sizeof(uint32_t), stream_));
@@ -1094,7 +1100,6 @@ sph_status StepState::read_scene(uint32_t scene, sph_dynamic_particle* out, floa
             accel_out[3ull * i + 2] = tmp[i].z;
         }
     }
-    CUDA_TRY(cudaStreamSynchronize(stream_));
     return check_device_error();
 }
 
@@ -1117,7 +1122,6 @@ sph_status StepState::write_scene(uint32_t scene, const sph_dynamic_particle* in
     if (st != SPH_OK) return st;
     st = enqueue_sort(0, /*keep_tags=*/true);
     if (st != SPH_OK) return st;
-    CUDA_TRY(cudaStreamSynchronize(stream_));
     return check_device_error();
 }
 
