@@ -282,6 +282,8 @@ def run_plain(args, world, rank, local, pg):
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                      "alg_bytes_per_launch": alg_bytes(dom_name, n, s)},
+        "issue_roofline": issue_roofline(dom_name, args.workload, float(stage_ms[dom]),
+                                         float(clk.get("sm_mhz") or 0.0) if isinstance(clk, dict) else 0.0),
         "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": 32 * n,
                 "d2h_bytes_per_step": 32 * n, "steps": e2e_steps},
         # per step: density, force, overflow force, scan, scatter, gather
@@ -321,21 +323,40 @@ def time_render(eng, scene, width: int = 1920, height: int = 1080, frames: int =
             "camera": "box x5, eye 8 units off its centre, fov 120 deg, sizes 0.1 / 0.03"}
 
 
-def profiled_traffic(stage: str, workload: str):
-    """DRAM bytes per launch of the kernel from the committed ncu summary
-    (profiles/ncu_traffic.txt, lines "workload stage bytes_per_launch")."""
+def profiled_traffic(stage: str, workload: str, column: int = 2):
+    """A per-launch figure of the kernel from the committed ncu summary
+    (profiles/ncu_traffic.txt, lines "workload stage dram_bytes
+    warp_instructions"): column 2 the DRAM bytes, column 3 the warp
+    instructions."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
     if not os.path.exists(path):
         return None
     with open(path) as f:
         for ln in f:
             parts = ln.split()
-            if len(parts) >= 3 and parts[0] == workload and parts[1] == stage:
+            if len(parts) > column and parts[0] == workload and parts[1] == stage:
                 try:
-                    return float(parts[2])
+                    return float(parts[column])
                 except ValueError:
                     return None
     return None
+
+
+def issue_roofline(stage: str, workload: str, stage_ms: float, sm_mhz: float):
+    """The bound the neighbour passes actually meet: warp instructions per
+    launch (ncu, committed) over the live launch time, against the issue
+    peak of 152 SMs x 4 schedulers x one warp instruction per cycle at the
+    SM clock sampled during the timed steps."""
+    inst = profiled_traffic(stage, workload, 3)
+    if inst is None or not sm_mhz:
+        return None
+    import torch
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    achieved = inst / (stage_ms * 1e-3)
+    peak = sms * 4 * sm_mhz * 1e6
+    return {"kernel": stage, "achieved": achieved, "peak": peak, "unit": "warp instructions/s",
+            "frac": achieved / peak, "warp_instructions_per_launch": inst,
+            "peak_basis": f"{sms} SMs x 4 schedulers x {sm_mhz:.0f} MHz"}
 
 
 def main():
