@@ -233,16 +233,18 @@ def run_plain(args, world, rank, local, pg):
     total_s = max_over_ranks(pg, total_s, local)
     value = world * n * args.steps / total_s
 
-    # per-stage times over the same number of steps (events around each stage)
+    # per-stage times over the same number of steps (events around each
+    # stage); the median per stage, so a step disturbed by the shared host
+    # does not skew the breakdown
     eng.set_timing(True)
-    stage_sum = np.zeros(5)
+    per_step = []
     for k in range(args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()
         eng.update(scene.dt, 1)
-        stage_sum += eng.kernel_times()
+        per_step.append(eng.kernel_times().astype(np.float64))
     eng.set_timing(False)
-    stage_ms = stage_sum / args.steps
+    stage_ms = np.median(np.asarray(per_step), axis=0)
     dom = int(np.argmax(stage_ms))
     dom_name = STAGES[dom]
     peak, peak_kind = measured_peaks()
