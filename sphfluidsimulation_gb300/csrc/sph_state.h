@@ -199,6 +199,7 @@ private:
     SortArgs sort_args(int kind) const;
     template <bool kExact>
     sph_status launch_step_staged(bool record_accel, bool timed);
+    unsigned overflow_grid(unsigned tiles_n);
     StepArgs step_args() const;
 
     int device_ = 0;
@@ -208,6 +209,7 @@ private:
     float stage_ms_[5] = {};
     uint32_t persistent_ctas_ = 0;
     bool exact_ = false;
+    uint32_t sm_count_ = 0;
     uint32_t grid_cache_ = 0;
     uint32_t cap_n_ = 0, cap_q_ = 0, cap_s_ = 0, cap_sq_ = 0, cap_sf_ = 0, cap_sbm_ = 0, cap_t_ = 0, max_scenes_ = 0,
              max_tiles_ = 0;

@@ -80,16 +80,19 @@ __global__ void __launch_bounds__(kTileThreads, SPH_FORCE_MIN_CTAS) k_force(Step
                                 nbr_args(a), force_out(a));
 }
 
-// Particles whose neighbour list overflowed; whole tiles without one exit at
-// once (the density pass records a per-tile flag).
+// Particles whose neighbour list overflowed.  A grid of a few CTAs per SM
+// walks the per-tile flags the density pass set, so a step without overflow
+// costs one flag read per tile.
 template <bool kRecord, bool kExact>
 __global__ void __launch_bounds__(kTileThreads) k_force_overflow(StepArgs a)
 {
-    if (a.tile_overflow[blockIdx.x] == 0u) return;
-    force_overflow_tile<kRecord, kExact>(a.tiles[blockIdx.x], a.scenes, a.pos, a.vel, a.tag, a.start,
-                                         static_tables(a), triangle_mesh(a), nbr_args(a), force_out(a));
-    __syncthreads();
-    if (threadIdx.x == 0) a.tile_overflow[blockIdx.x] = 0u;   // every thread has read the flag
+    for (uint32_t t = blockIdx.x; t < a.num_tiles; t += gridDim.x) {
+        if (a.tile_overflow[t] == 0u) continue;                  // the same for the whole CTA
+        force_overflow_tile<kRecord, kExact>(a.tiles[t], a.scenes, a.pos, a.vel, a.tag, a.start,
+                                             static_tables(a), triangle_mesh(a), nbr_args(a), force_out(a));
+        __syncthreads();
+        if (threadIdx.x == 0) a.tile_overflow[t] = 0u;            // every thread has read the flag
+    }
 }
 
 // Bounded grid barrier for the persistent kernel (all CTAs co-resident by
@@ -908,10 +911,10 @@ sph_status StepState::launch_step_staged(bool record_accel, bool timed)
     if (timed) CUDA_TRY(cudaEventRecord(events_[1], stream_));
     if (record_accel) {
         k_force<true, kExact><<<nt, kTileThreads, 0, stream_>>>(a);
-        k_force_overflow<true, kExact><<<nt, kTileThreads, 0, stream_>>>(a);
+        k_force_overflow<true, kExact><<<overflow_grid(nt), kTileThreads, 0, stream_>>>(a);
     } else {
         k_force<false, kExact><<<nt, kTileThreads, 0, stream_>>>(a);
-        k_force_overflow<false, kExact><<<nt, kTileThreads, 0, stream_>>>(a);
+        k_force_overflow<false, kExact><<<overflow_grid(nt), kTileThreads, 0, stream_>>>(a);
     }
     CUDA_TRY(cudaGetLastError());
     if (timed) CUDA_TRY(cudaEventRecord(events_[2], stream_));
@@ -925,6 +928,17 @@ sph_status StepState::launch_step_staged(bool record_accel, bool timed)
     CUDA_TRY(cudaGetLastError());
     if (timed) CUDA_TRY(cudaEventRecord(events_[5], stream_));
     return SPH_OK;
+}
+
+// Grid of the overflow force pass: four CTAs per SM, at most one per tile.
+unsigned StepState::overflow_grid(unsigned tiles_n)
+{
+    if (!sm_count_) {
+        int sms = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_) != cudaSuccess || sms < 1) sms = 1;
+        sm_count_ = (uint32_t)sms;
+    }
+    return std::max(1u, std::min(tiles_n, 4u * sm_count_));
 }
 
 sph_status StepState::enqueue_step_staged(bool record_accel, bool timed)
