@@ -268,6 +268,10 @@ SPH_API sph_status sph_batch_finalize(sph_batch* batch);
 SPH_API sph_status sph_batch_step(sph_batch* batch, uint32_t steps);
 SPH_API sph_status sph_batch_set_mode(sph_batch* batch, int mode);
 
+/* Neighbour-pass arithmetic of every scene, as sph_engine_set_exact: with
+ * exact = 1 each scene's bytes equal the reference CPU engine's. */
+SPH_API sph_status sph_batch_set_exact(sph_batch* batch, int exact);
+
 /* Autotuner: times trial_steps steps of each configuration -- the staged
  * step graph, and the persistent kernel at 1, 2, ... CTAs per SM up to its
  * occupancy limit -- on a saved copy of the state (restored after each
@@ -307,6 +311,9 @@ SPH_API sph_status sph_server_submit(sph_server* server, const sph_params* param
  * retires finished jobs.  *active and *queued report the state afterwards. */
 SPH_API sph_status sph_server_poll(sph_server* server, uint32_t chunk_steps, uint32_t* active,
                                    uint32_t* queued);
+
+/* Neighbour-pass arithmetic of every job, as sph_engine_set_exact. */
+SPH_API sph_status sph_server_set_exact(sph_server* server, int exact);
 
 /* Retrieves a finished job's particles (input order, n entries) and
  * densities (n floats, rho = p/k + rho0); may be NULL.  Returns

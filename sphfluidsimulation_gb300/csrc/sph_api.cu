@@ -475,6 +475,15 @@ SPH_API sph_status sph_batch_set_mode(sph_batch* b, int mode)
     return SPH_OK;
 }
 
+SPH_API sph_status sph_batch_set_exact(sph_batch* b, int exact)
+{
+    if (!b) return SPH_ERR_INVALID_ARGUMENT;
+    API_CUDA_TRY(cudaSetDevice(b->device));
+    API_CUDA_TRY(cudaStreamSynchronize(b->stream));
+    b->state.set_exact(exact != 0);
+    return SPH_OK;
+}
+
 SPH_API sph_status sph_batch_step(sph_batch* b, uint32_t steps)
 {
     if (!b) return SPH_ERR_INVALID_ARGUMENT;

@@ -340,6 +340,15 @@ SPH_API sph_status sph_server_submit(sph_server* sv, const sph_params* params, c
     return SPH_OK;
 }
 
+SPH_API sph_status sph_server_set_exact(sph_server* sv, int exact)
+{
+    if (!sv) return SPH_ERR_INVALID_ARGUMENT;
+    SRV_CUDA_TRY(cudaSetDevice(sv->device));
+    SRV_CUDA_TRY(cudaStreamSynchronize(sv->stream));
+    sv->arena.set_exact(exact != 0);
+    return SPH_OK;
+}
+
 SPH_API sph_status sph_server_poll(sph_server* sv, uint32_t chunk_steps, uint32_t* active_out, uint32_t* queued_out)
 {
     if (!sv || chunk_steps == 0) return SPH_ERR_INVALID_ARGUMENT;

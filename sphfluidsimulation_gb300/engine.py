@@ -254,6 +254,9 @@ class Batch:
     def set_mode(self, mode: int) -> None:
         check(self.lib.sph_batch_set_mode(self.h, int(mode)), "sph_batch_set_mode")
 
+    def set_exact(self, exact: bool = True) -> None:
+        check(self.lib.sph_batch_set_exact(self.h, int(exact)), "sph_batch_set_exact")
+
     def step(self, steps: int = 1) -> None:
         check(self.lib.sph_batch_step(self.h, int(steps)), "sph_batch_step")
 
@@ -319,6 +322,9 @@ class Server:
               "sph_server_submit")
         self.sizes[jid.value] = n
         return jid.value
+
+    def set_exact(self, exact: bool = True) -> None:
+        check(self.lib.sph_server_set_exact(self.h, int(exact)), "sph_server_set_exact")
 
     def poll(self, chunk_steps: int = 50):
         a = C.c_uint32()

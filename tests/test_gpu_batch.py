@@ -81,3 +81,28 @@ def test_autotune_keeps_state_and_results():
     b.step(12)
     for sid, sc in zip(ids, scs):
         assert b.read_scene(sid).tobytes() == alone(sc, 12).tobytes(), sc.name
+
+
+def test_batch_exact_arithmetic_equals_the_oracle():
+    """With the reference's arithmetic every scene of a batch reproduces the
+    reference CPU engine's bytes (the oracle, pinned to it), in both modes."""
+    import sys, os
+    sys.path.insert(0, os.path.dirname(__file__))
+    from oracle_lib import Oracle
+    scs = uneven_scenes()[:4]
+    for mode in (0, 1):
+        b = Batch()
+        ids = [b.add_scene(sc) for sc in scs]
+        b.finalize()
+        b.set_mode(mode)
+        b.set_exact(True)
+        b.step(6)
+        b.step(5)
+        for sid, sc in zip(ids, scs):
+            o = Oracle(0)
+            o.init(sc)
+            o.update(sc.dt, 11)
+            _, _, io = o.maps()
+            ref = np.empty(sc.n, o.read_raw().dtype)
+            ref[io] = o.read_raw()
+            assert b.read_scene(sid).tobytes() == ref.tobytes(), (mode, sc.name)

@@ -80,3 +80,35 @@ def test_malformed_jobs_rejected():
         srv.submit(sc)
     with pytest.raises(SphError):
         Server(budget_bytes=0)
+
+
+def test_served_exact_arithmetic_equals_the_oracle():
+    """Jobs served with the reference's arithmetic return the reference CPU
+    engine's bytes (the oracle), whatever the mix and the poll chunks."""
+    import os, sys
+    sys.path.insert(0, os.path.dirname(__file__))
+    from oracle_lib import Oracle
+    specs = [(1500, 13, 11), (800, 21, 12), (2600, 8, 13)]
+    scs = [job(n, st, sd) for n, st, sd in specs]
+    srv = Server(budget_bytes=1 << 30, max_slots=4)
+    srv.set_exact(True)
+    ids = [srv.submit(sc) for sc in scs]
+    done = {}
+    for _ in range(100):
+        a, q = srv.poll(6)
+        for jid in ids:
+            if jid not in done:
+                r = srv.result(jid)
+                if r is not None:
+                    done[jid] = r
+        if len(done) == len(ids):
+            break
+    assert len(done) == len(ids)
+    for jid, sc in zip(ids, scs):
+        o = Oracle(0)
+        o.init(sc)
+        o.update(sc.dt, sc.steps)
+        _, _, io = o.maps()
+        ref = np.empty(sc.n, o.read_raw().dtype)
+        ref[io] = o.read_raw()
+        assert done[jid][0].tobytes() == ref.tobytes(), sc.name
