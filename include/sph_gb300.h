@@ -181,6 +181,16 @@ SPH_API sph_status sph_engine_kernel_times(sph_engine* engine, float* ms, int co
  * own work or timing events with the engine's launches. */
 SPH_API sph_status sph_engine_get_stream(sph_engine* engine, void** stream);
 
+/* Failure-detection test hook.  Every device wait of the engine (the scan's
+ * look-back, the persistent step's grid barrier) gives up after a bounded
+ * number of polls, sets a bit in a device status word and lets the kernel
+ * finish; the host then reports SPH_ERR_DEVICE_TIMEOUT and the context stays
+ * usable.  This call makes one such wait run out: the scan kernel runs for a
+ * tile whose predecessor is never published.  It returns
+ * SPH_ERR_DEVICE_TIMEOUT with the status bits (1 = scan wait expired) after
+ * about a second. */
+SPH_API sph_status sph_debug_expire_wait(int device, uint32_t* status_bits);
+
 /* ---- headless particle rendering ----------------------------------------
  * The reference's particle renderer (ParticleRenderer.cpp:75-82 with
  * Shaders/particle.vert:67-117 and particle.frag:17-22) without a graphics

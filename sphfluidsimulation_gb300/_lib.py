@@ -70,6 +70,7 @@ _SIGS = {
     "sph_engine_count": (_st, [_vp, C.c_int, _u64p]),
     "sph_engine_record_acceleration": (_st, [_vp, C.c_int]),
     "sph_engine_set_exact": (_st, [_vp, C.c_int]),
+    "sph_debug_expire_wait": (_st, [C.c_int, _up]),
     "sph_batch_set_exact": (_st, [_vp, C.c_int]),
     "sph_server_set_exact": (_st, [_vp, C.c_int]),
     "sph_engine_render": (_st, [_vp, C.POINTER(SphRenderView), C.POINTER(SphRenderLayer), C.POINTER(SphRenderLayer),

@@ -266,6 +266,13 @@ SPH_API sph_status sph_engine_render(sph_engine* e, const sph_render_view* view,
     return e->state.render(*view, dynamic_layer, static_layer, rgba, depth);
 }
 
+SPH_API sph_status sph_debug_expire_wait(int device, uint32_t* status_bits)
+{
+    if (!status_bits) return SPH_ERR_INVALID_ARGUMENT;
+    *status_bits = 0;
+    return sph::scan_wait_probe(device, status_bits);
+}
+
 SPH_API sph_status sph_engine_set_exact(sph_engine* e, int exact)
 {
     if (!e) return SPH_ERR_INVALID_ARGUMENT;

@@ -71,6 +71,8 @@ inline sph_status dev_alloc(T** p, size_t count)
 }
 
 sph_status validate_scene(const SceneInput& in);
+// Makes the scan's bounded look-back expire on purpose (see sph_step.cu).
+sph_status scan_wait_probe(int device, uint32_t* status_bits);
 // Physics constants and sizes of a scene (offsets left zero).
 SceneDesc scene_desc_for(const SceneInput& in);
 

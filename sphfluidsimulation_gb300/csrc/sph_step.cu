@@ -214,6 +214,46 @@ __global__ void __launch_bounds__(kTileThreads) k_load(const Tile* tiles, const 
 // StepState host side
 // ---------------------------------------------------------------------------
 
+// Failure-detection probe: the scan kernel on two tiles of zeros, launched for
+// tile 1 alone (the ticket starts at 1), so tile 1's look-back waits for a tile
+// 0 that is never published.  The bounded wait expires, sets the status bit
+// and lets the kernel finish; every access stays inside the probe's arrays.
+sph_status scan_wait_probe(int device, uint32_t* status_bits)
+{
+    CUDA_TRY(cudaSetDevice(device));
+    const uint32_t len = 2u * kScanTile;
+    uint32_t *cnt = nullptr, *out = nullptr, *ticket = nullptr, *err = nullptr;
+    unsigned long long* status = nullptr;
+    sph_status st = SPH_OK;
+    if ((st = dev_alloc(&cnt, len)) == SPH_OK && (st = dev_alloc(&out, len)) == SPH_OK &&
+        (st = dev_alloc(&ticket, 1)) == SPH_OK && (st = dev_alloc(&err, 1)) == SPH_OK &&
+        (st = dev_alloc(&status, 2)) == SPH_OK) {
+        const uint32_t one = 1u;
+        cudaError_t e = cudaMemset(cnt, 0, sizeof(uint32_t) * len);
+        if (e == cudaSuccess) e = cudaMemset(status, 0, sizeof(unsigned long long) * 2);
+        if (e == cudaSuccess) e = cudaMemset(err, 0, sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMemcpy(ticket, &one, sizeof(uint32_t), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) {
+            k_scan<<<1, kScanThreads>>>(cnt, out, len, status, ticket, err);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        if (e == cudaSuccess) e = cudaMemcpy(status_bits, err, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            set_last_error(std::string("wait probe: ") + cudaGetErrorString(e));
+            st = SPH_ERR_CUDA;
+        }
+    }
+    for (void* p : {(void*)cnt, (void*)out, (void*)ticket, (void*)err, (void*)status})
+        if (p) cudaFree(p);
+    if (st != SPH_OK) return st;
+    if (*status_bits & DEV_ERR_SCAN_TIMEOUT) {
+        set_last_error("device status 0x1 (scan wait expired)");
+        return SPH_ERR_DEVICE_TIMEOUT;
+    }
+    return SPH_OK;
+}
+
 thread_local std::string g_last_error;
 
 void set_last_error(const std::string& s) { g_last_error = s; }
