@@ -3,13 +3,18 @@ break (FP32), through the engine's C ABI, plus the batched and served forms.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                     [--workload dam_break_1m|dam_break_16k|pool_drop_8m|batched|served]
+                    [--dt SECONDS]
 
 One JSON line on stdout (rank 0).  A "step" is one SPH step of the whole
 scene: density, force/integrate, scan, scatter, gather.  The device-resident
 value is timed with CUDA events on the engine's stream, one step at a time,
 with L2 flushed (256 MiB write) before each timed step; e2e repeats the step
 through the C ABI with the particle state copied in from pinned host memory
-and read back each step.  With --gpus N (torchrun) every rank advances its own
+and read back each step.  The scenes run at their configured step of 1e-4 s
+unless --dt says otherwise; at the 1M and 8M scenes' smoothing radii that
+step makes the viscosity term diverge within tens of steps (in the
+reference's arithmetic too), so the timed window covers the onset of the
+divergence.  With --gpus N (torchrun) every rank advances its own
 replica of the scene (the path does not shard); value = all ranks' particle-
 steps / max rank time.
 """
@@ -42,15 +47,22 @@ def measured_peaks():
     return HBM_FALLBACK_GBS, "fallback"
 
 
-def workload_scene(name: str, steps: int):
+def workload_scene(name: str, steps: int, dt=None):
+    """The named scene; ``dt`` replaces its time step when given (the
+    configured 1e-4 s diverges at the 1M and 8M scenes' h; scenes.STABLE_DT
+    holds the stable steps)."""
     from sphfluidsimulation_gb300 import scenes
     if name == "dam_break_1m":
-        return scenes.config1(steps)
-    if name == "dam_break_16k":
-        return scenes.config0(steps)
-    if name == "pool_drop_8m":
-        return scenes.config2(steps)
-    raise ValueError(name)
+        sc = scenes.config1(steps)
+    elif name == "dam_break_16k":
+        sc = scenes.config0(steps)
+    elif name == "pool_drop_8m":
+        sc = scenes.config2(steps)
+    else:
+        raise ValueError(name)
+    if dt is not None:
+        sc.dt = float(dt)
+    return sc
 
 
 def alg_bytes(stage: str, n: int, s: int) -> float:
@@ -64,7 +76,8 @@ def alg_bytes(stage: str, n: int, s: int) -> float:
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks / throttle reasons sampled every 25 ms (the timed
+    region of the default run lasts a few tens of ms)."""
 
     FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active," \
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown," \
@@ -79,7 +92,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "25"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -170,7 +183,8 @@ def run_reference(args):
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    scene = workload_scene(args.workload if args.workload not in ("batched", "served") else "dam_break_1m", 1)
+    scene = workload_scene(args.workload if args.workload not in ("batched", "served") else "dam_break_1m", 1,
+                           args.dt)
     # bounded sample: the steps of this run, capped at about a minute of CPU work
     warm = 1
     value, secs, steps = cpu_baseline(scene, 60.0, args.steps, threads)
@@ -200,7 +214,7 @@ def run_plain(args, world, rank, local, pg):
     from sphfluidsimulation_gb300.engine import DYN_DTYPE, SimulationEngineCUDA
 
     torch.cuda.set_device(local)
-    scene = workload_scene(args.workload, args.steps)
+    scene = workload_scene(args.workload, args.steps, args.dt)
     n, s = scene.n, scene.s
     eng = SimulationEngineCUDA(local)
     eng.initialize(scene)
@@ -369,6 +383,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="dam_break_1m",
                     choices=["dam_break_1m", "dam_break_16k", "pool_drop_8m", "batched", "served"])
+    ap.add_argument("--dt", type=float, default=None,
+                    help="time step in s (default: the workload's configured 1e-4)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the bounded batched/served samples in the default line")

@@ -192,10 +192,11 @@ def config0(steps: int = 200) -> Scene:
     return dam_break((32, 16, 32), 0.02, 0.04, (1.0, 0.6, 0.7), steps, mass=0.008, name="dam_break_16k")
 
 
-def config1(steps: int = 1000) -> Scene:
+def config1(steps: int = 1000, dt: float = 1e-4) -> Scene:
     """1,048,576 particles: 128 (x) x 64 (y) x 128 (z) at 0.005, h 0.01, in a
-    1.6 x 0.8 x 0.8 box (256,002 wall particles)."""
-    return dam_break((128, 64, 128), 0.005, 0.01, (1.6, 0.8, 0.8), steps, name="dam_break_1m")
+    1.6 x 0.8 x 0.8 box (256,002 wall particles).  dt defaults to the
+    dam-break 1e-4 s, which diverges at this h (see STABLE_DT)."""
+    return dam_break((128, 64, 128), 0.005, 0.01, (1.6, 0.8, 0.8), steps, name="dam_break_1m", dt=dt)
 
 
 def pool_drop(pool_lattice: Sequence[int], n_total: int, box: Sequence[float], steps: int,
@@ -229,20 +230,22 @@ def pool_drop(pool_lattice: Sequence[int], n_total: int, box: Sequence[float], s
     return Scene(name=name, dyn_pos=dyn, static_pos=walls, params=water_params(s, h), dt=dt, steps=steps)
 
 
-# Explicit viscosity is stable only for dt below about h^2 / (8 mu): with
-# mu = 0.1 that is 1.25e-4 s at h = 0.01 but 3.1e-5 s at h = 0.005, where the
-# dam-break dt of 1e-4 s makes every particle leave its cell on every step
-# within five steps (and the reference's arithmetic diverges alike).
-POOL_DROP_STABLE_DT = 2.5e-5
+# The explicit viscosity term bounds the step like h^2 / mu.  With mu = 0.1
+# the dam-break dt of 1e-4 s is stable at h = 0.04 (configuration 0) but
+# diverges at h = 0.01 (the 1M dam break: median speed 30 m/s by step 20)
+# and at h = 0.005 (the 8M pool drop: every particle leaves its cell on every
+# step from step 4), in the reference's arithmetic as in this engine's.
+# These are the largest halvings of 1e-4 s that stay stable at those h,
+# measured with the oracle (at h = 0.01, 1e-4 s with mu = 0 is stable too).
+STABLE_DT = {"dam_break_1m": 5e-5, "pool_drop_8m": 2.5e-5}
 
 
-def config2(steps: int = 500, seed: int = 0, dt: float = POOL_DROP_STABLE_DT) -> Scene:
+def config2(steps: int = 500, seed: int = 0, dt: float = 1e-4) -> Scene:
     """8,388,608 particles: a 256 (x) x 112 (y) x 256 (z) pool at 0.0025 plus
     the 1,048,576 lattice points nearest the centre of a sphere whose bottom
     is 0.3 m above the pool; box 1.28 (x) x 1.28 (y) x 0.96 (z); h 0.005 and
-    the dam-break constants.  dt defaults to 2.5e-5 s, the largest quarter of
-    the dam-break 1e-4 s inside the viscous limit at this h; ``dt=1e-4``
-    gives the literal dam-break step, which diverges."""
+    the dam-break constants.  dt defaults to the dam-break 1e-4 s, which
+    diverges at this h (see STABLE_DT)."""
     return pool_drop((256, 112, 256), 8_388_608, (1.28, 1.28, 0.96), steps, seed=seed, dt=dt,
                      name="pool_drop_8m")
 

@@ -222,7 +222,7 @@ def test_pool_drop_8m_exact_and_default_arithmetic():
     particle; the default arithmetic stays within the density (1e-5
     relative) and position (1e-3 h RMS) tolerances; and the bucket table
     holds the reference's invariants."""
-    sc = scenes.config2(steps=0)
+    sc = scenes.config2(steps=0, dt=scenes.STABLE_DT["pool_drop_8m"])
     o = Oracle(0)
     o.init(sc)
     o.update(sc.dt, 2)
