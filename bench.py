@@ -75,6 +75,29 @@ def alg_bytes(stage: str, n: int, s: int) -> float:
     return per * n + extra
 
 
+def pair_rates(samples, stage_ms, first_step: int):
+    """Candidate tests and in-range pairs per particle (means of
+    sph_engine_neighbour_stats samples over the stage-timing steps) and the
+    rates they imply: density tests `candidates` pairs against h, force
+    evaluates the in-range ones."""
+    if not samples:
+        return None
+    mean = {k: float(np.mean([s[k] for s in samples])) for k in samples[0]}
+    n = max(mean["particles"], 1.0)
+    dens_s = float(stage_ms[STAGES.index("density")]) * 1e-3
+    force_s = float(stage_ms[STAGES.index("force")]) * 1e-3
+    in_range = mean["neighbours"] + mean["static_neighbours"]
+    return {
+        "candidates_per_particle": mean["candidates"] / n,
+        "warp_slots_per_particle": mean["warp_slots"] / n,
+        "neighbours_per_particle": mean["neighbours"] / n,
+        "static_neighbours_per_particle": mean["static_neighbours"] / n,
+        "density_candidate_tests_per_s": mean["candidates"] / dens_s if dens_s > 0 else None,
+        "force_pair_evals_per_s": in_range / force_s if force_s > 0 else None,
+        "steps_sampled": f"{first_step}..{first_step + 10 * (len(samples) - 1)} every 10",
+    }
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 25 ms (the timed
     region of the default run lasts a few tens of ms)."""
@@ -251,14 +274,17 @@ def run_plain(args, world, rank, local, pg):
     # stage); the median per stage, so a step disturbed by the shared host
     # does not skew the breakdown
     eng.set_timing(True)
-    per_step = []
+    per_step, nstats = [], []
     for k in range(args.steps):
+        if k % 10 == 0:                           # the walk's counts over the same states
+            nstats.append(eng.neighbour_stats())
         with torch.cuda.stream(stream):
             flush.zero_()
         eng.update(scene.dt, 1)
         per_step.append(eng.kernel_times().astype(np.float64))
     eng.set_timing(False)
     stage_ms = np.median(np.asarray(per_step), axis=0)
+    pairs = pair_rates(nstats, stage_ms, args.warmup + args.steps)
     dom = int(np.argmax(stage_ms))
     dom_name = STAGES[dom]
     peak, peak_kind = measured_peaks()
@@ -298,6 +324,7 @@ def run_plain(args, world, rank, local, pg):
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                      "alg_bytes_per_launch": alg_bytes(dom_name, n, s)},
+        "pairs": pairs,
         "issue_roofline": issue_roofline(dom_name, args.workload, float(stage_ms[dom]),
                                          float(clk.get("sm_mhz") or 0.0) if isinstance(clk, dict) else 0.0),
         "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": 32 * n,

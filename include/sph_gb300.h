@@ -177,6 +177,23 @@ SPH_API sph_status sph_engine_read_acceleration(sph_engine* engine, float* out);
 SPH_API sph_status sph_engine_set_timing(sph_engine* engine, int on);
 SPH_API sph_status sph_engine_kernel_times(sph_engine* engine, float* ms, int count);
 
+/* Neighbour statistics of the current state, for measurement (one extra
+ * launch and a synchronisation; no effect on the simulation).  The density
+ * pass tests every dynamic particle of the 27 neighbour buckets it does not
+ * skip (SF:397-495 tests all of them): `candidates` counts those tests and
+ * `warp_slots` the lane-slots a warp spends on them, since each bucket costs
+ * a warp its largest member count.  `neighbours` counts dynamic pairs
+ * within h (each ordered pair once), `static_neighbours` static particles
+ * within h of a dynamic one. */
+typedef struct sph_neighbour_stats {
+    uint64_t particles;
+    uint64_t candidates;
+    uint64_t warp_slots;
+    uint64_t neighbours;
+    uint64_t static_neighbours;
+} sph_neighbour_stats;
+SPH_API sph_status sph_engine_neighbour_stats(sph_engine* engine, sph_neighbour_stats* out);
+
 /* The engine's CUDA stream (a cudaStream_t), for callers that order their
  * own work or timing events with the engine's launches. */
 SPH_API sph_status sph_engine_get_stream(sph_engine* engine, void** stream);

@@ -38,6 +38,11 @@ class SphRenderLayer(C.Structure):
     _fields_ = [("size", C.c_float), ("color", C.c_float * 4)]
 
 
+class SphNeighbourStats(C.Structure):
+    _fields_ = [("particles", C.c_uint64), ("candidates", C.c_uint64), ("warp_slots", C.c_uint64),
+                ("neighbours", C.c_uint64), ("static_neighbours", C.c_uint64)]
+
+
 STATUS = {0: "SPH_OK", 1: "SPH_ERR_INVALID_ARGUMENT", 2: "SPH_ERR_NOT_INITIALIZED", 3: "SPH_ERR_CUDA",
           4: "SPH_ERR_OUT_OF_MEMORY", 5: "SPH_ERR_DEVICE_TIMEOUT", 6: "SPH_ERR_CAPACITY", 7: "SPH_ERR_BUDGET",
           8: "SPH_ERR_NOT_FOUND"}
@@ -78,6 +83,7 @@ _SIGS = {
     "sph_engine_read_acceleration": (_st, [_vp, _fp]),
     "sph_engine_set_timing": (_st, [_vp, C.c_int]),
     "sph_engine_kernel_times": (_st, [_vp, _fp, C.c_int]),
+    "sph_engine_neighbour_stats": (_st, [_vp, C.POINTER(SphNeighbourStats)]),
     "sph_engine_get_stream": (_st, [_vp, C.POINTER(_vp)]),
     "sph_cell_sort": (_st, [C.c_int, _fp, C.c_uint32, C.c_float, C.c_uint32, _up, _up, _up, _up]),
     "sph_cell_sort_noalloc": (_st, [_vp, C.c_uint32, C.c_float, C.c_uint32, _vp, _vp, _vp, _vp]),

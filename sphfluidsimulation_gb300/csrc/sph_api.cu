@@ -318,6 +318,21 @@ SPH_API sph_status sph_engine_kernel_times(sph_engine* e, float* ms, int count)
     return SPH_OK;
 }
 
+SPH_API sph_status sph_engine_neighbour_stats(sph_engine* e, sph_neighbour_stats* out)
+{
+    if (!e || !out) return SPH_ERR_INVALID_ARGUMENT;
+    if (!e->initialized) return SPH_ERR_NOT_INITIALIZED;
+    API_CUDA_TRY(cudaSetDevice(e->device));
+    uint64_t v[5];
+    API_TRY(e->state.neighbour_stats(v));
+    out->particles = v[0];
+    out->candidates = v[1];
+    out->warp_slots = v[2];
+    out->neighbours = v[3];
+    out->static_neighbours = v[4];
+    return SPH_OK;
+}
+
 SPH_API sph_status sph_engine_get_stream(sph_engine* e, void** stream)
 {
     if (!e || !stream) return SPH_ERR_INVALID_ARGUMENT;

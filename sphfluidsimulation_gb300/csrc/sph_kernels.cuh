@@ -589,10 +589,14 @@ __device__ __forceinline__ Walk make_walk(const SceneDesc& sc, const float4& p, 
 // r2)).  Dynamic and static sums are separate in the reference, so only the
 // order inside each kind matters.  Cells whose box lies beyond h are skipped
 // when their bucket cannot hold another visited cell's particles.
-template <bool kExact, typename FD, typename FS>
-__device__ __forceinline__ void walk_neighbours(const SceneDesc& sc, uint32_t i, const float4& p, const Walk& w,
-                                                const float4* __restrict__ pos, const uint32_t* __restrict__ start,
-                                                const StaticTables& st, FD&& on_dyn, FS&& on_static)
+// on_cell(members) follows each cell's dynamic bucket with the number of
+// candidates tested there (0 when skipped); every lane of a warp calls it
+// 27 times in the same order.
+template <bool kExact, typename FD, typename FS, typename FC>
+__device__ __forceinline__ void walk_neighbours_cells(const SceneDesc& sc, uint32_t i, const float4& p,
+                                                      const Walk& w, const float4* __restrict__ pos,
+                                                      const uint32_t* __restrict__ start, const StaticTables& st,
+                                                      FD&& on_dyn, FS&& on_static, FC&& on_cell)
 {
     const float h2 = sc.h2;
     const float cull2 = __fmul_rn(h2, 1.0001f);
@@ -610,6 +614,7 @@ __device__ __forceinline__ void walk_neighbours(const SceneDesc& sc, uint32_t i,
                                   pick3f(c, w.box.z0, 0.f, w.box.z2);
                 const bool far = bd2 > cull2;
                 const uint32_t hsh = neighbour_hash(w.nb, a, b, c);
+                uint32_t members = 0;
                 if (!(far && w.cull_d)) {
                     const uint32_t bk = sc.q_off + fast_mod(hsh, sc.fm_b);
                     const uint32_t beg = max(__ldg(start + bk) + delta, sc.p_off);
@@ -619,7 +624,9 @@ __device__ __forceinline__ void walk_neighbours(const SceneDesc& sc, uint32_t i,
                         const float r2 = pair_r2<kExact>(q, p);
                         if (r2 <= h2 && j != i) on_dyn(j, q, r2);
                     }
+                    members = end > beg ? end - beg : 0u;
                 }
+                on_cell(members);
                 if (!w.near_static) continue;
                 if (w.ref_walk) {
                     // SF:454-490: bucket hash % s of the reference's table, every member
@@ -644,6 +651,14 @@ __device__ __forceinline__ void walk_neighbours(const SceneDesc& sc, uint32_t i,
                     }
                 }
             }
+}
+
+template <bool kExact, typename FD, typename FS>
+__device__ __forceinline__ void walk_neighbours(const SceneDesc& sc, uint32_t i, const float4& p, const Walk& w,
+                                                const float4* __restrict__ pos, const uint32_t* __restrict__ start,
+                                                const StaticTables& st, FD&& on_dyn, FS&& on_static)
+{
+    walk_neighbours_cells<kExact>(sc, i, p, w, pos, start, st, on_dyn, on_static, [](uint32_t) {});
 }
 
 // Position of a static list entry.

@@ -110,6 +110,9 @@ public:
     sph_status write_scene(uint32_t scene, const sph_dynamic_particle* in);
     sph_status read_static(uint32_t scene, sph_static_particle* out, uint32_t* bucket_starts);
     sph_status read_buckets(uint32_t scene, uint32_t* bucket_starts, uint32_t* slot_ids);
+    // particles, candidates, warp candidate slots, dynamic and static
+    // neighbours within h, summed over all scenes (k_neighbour_stats)
+    sph_status neighbour_stats(uint64_t out[5]);
     sph_status persistent_grid(uint32_t* grid);
     // Outputs of the initial sort of scene 0 (see sph_cell_sort).
     sph_status read_sort(uint32_t* keys, uint32_t* counts, uint32_t* starts, uint32_t* order);

@@ -95,6 +95,39 @@ __global__ void __launch_bounds__(kTileThreads) k_force_overflow(StepArgs a)
     }
 }
 
+// Neighbour statistics of the current state (a measurement, run outside the
+// step): out[0] particles; out[1] dynamic candidates the density walk tests;
+// out[2] the candidate slots the warps spend on them (a cell costs a warp its
+// largest bucket, so out[2] / out[1] is the divergence overhead); out[3]
+// dynamic neighbours within h (each ordered pair once); out[4] static
+// particles within h of a dynamic one.
+__global__ void __launch_bounds__(kTileThreads) k_neighbour_stats(StepArgs a, unsigned long long* out)
+{
+    const Tile& tile = a.tiles[blockIdx.x];
+    const SceneDesc& sc = a.scenes[tile.scene];
+    const uint32_t i = tile.begin + threadIdx.x;
+    const bool valid = i < tile.end;
+    const unsigned mask = __ballot_sync(0xffffffffu, valid);
+    unsigned long long v[5] = {valid ? 1ull : 0ull, 0ull, 0ull, 0ull, 0ull};
+    if (valid) {
+        const float4 p = a.pos[i];
+        const Walk w = make_walk<false>(sc, p, a.sbitmap);
+        walk_neighbours_cells<false>(
+            sc, i, p, w, a.pos, a.start, static_tables(a),
+            [&](uint32_t, const float4&, float) { ++v[3]; },
+            [&](uint32_t, const float4&, float) { ++v[4]; },
+            [&](uint32_t m) {               // every valid lane, 27 times, in step
+                v[1] += m;
+                v[2] += __reduce_max_sync(mask, m);
+            });
+    }
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    if ((threadIdx.x & 31u) == 0u && mask)
+        for (int k = 0; k < 5; ++k) atomicAdd(out + k, v[k]);
+}
+
 // Bounded grid barrier for the persistent kernel (all CTAs co-resident by
 // cooperative launch).  Sense by generation counter; on expiry the error word
 // is set and the CTA proceeds, so the launch always terminates.
@@ -1197,6 +1230,30 @@ sph_status StepState::read_static(uint32_t scene, sph_static_particle* out, uint
         for (uint32_t k = 0; k <= d.s; ++k) bucket_starts[k] -= b0;
     }
     return SPH_OK;
+}
+
+sph_status StepState::neighbour_stats(uint64_t out[5])
+{
+    for (int k = 0; k < 5; ++k) out[k] = 0;
+    if (tiles.empty()) return SPH_OK;
+    unsigned long long* d = nullptr;
+    sph_status st = dev_alloc(&d, 5);
+    if (st != SPH_OK) return st;
+    unsigned long long h[5] = {};
+    cudaError_t e = cudaMemsetAsync(d, 0, sizeof h, stream_);
+    if (e == cudaSuccess) {
+        k_neighbour_stats<<<(unsigned)tiles.size(), kTileThreads, 0, stream_>>>(step_args(), d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, sizeof h, cudaMemcpyDeviceToHost, stream_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
+    cudaFree(d);
+    if (e != cudaSuccess) {
+        set_last_error(std::string("neighbour statistics: ") + cudaGetErrorString(e));
+        return SPH_ERR_CUDA;
+    }
+    for (int k = 0; k < 5; ++k) out[k] = h[k];
+    return check_device_error();
 }
 
 sph_status StepState::read_buckets(uint32_t scene, uint32_t* bucket_starts, uint32_t* slot_ids)

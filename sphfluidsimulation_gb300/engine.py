@@ -197,6 +197,13 @@ class SimulationEngineCUDA:
         check(self.lib.sph_engine_kernel_times(self.h, _fptr(ms), 5), "sph_engine_kernel_times")
         return ms
 
+    def neighbour_stats(self) -> dict:
+        """Counts over the current state (sph_engine_neighbour_stats):
+        particles, candidates, warp_slots, neighbours, static_neighbours."""
+        st = _lib.SphNeighbourStats()
+        check(self.lib.sph_engine_neighbour_stats(self.h, C.byref(st)), "sph_engine_neighbour_stats")
+        return {name: int(getattr(st, name)) for name, _ in st._fields_}
+
 
 def cell_sort(pos: np.ndarray, h: float, buckets: int, device: int = 0):
     """The counting-sort stage alone: (keys, counts, starts, order)."""

@@ -273,3 +273,100 @@ def test_kernel_timing_reported():
     e.update(sc.dt, 3)
     t = e.kernel_times()
     assert (t > 0).all()
+
+
+def _expand_bits(v):
+    v = np.asarray(v, np.uint64) & np.uint64(0x3FF)
+    v = (v * np.uint64(0x00010001)) & np.uint64(0xFF0000FF)
+    v = (v * np.uint64(0x00000101)) & np.uint64(0x0F00F00F)
+    v = (v * np.uint64(0x00000011)) & np.uint64(0xC30C30C3)
+    v = (v * np.uint64(0x00000005)) & np.uint64(0x49249249)
+    return v
+
+
+def host_neighbour_stats(pos_sorted, starts, h):
+    """The density walk's counts rebuilt on the host: per particle the
+    members of every neighbour bucket it does not skip (a cell whose box
+    lies beyond h, when the 27 Morton codes span fewer than 2n), and per warp
+    of 32 slots each cell's largest such count."""
+    from scipy.spatial import cKDTree
+    n = pos_sorted.shape[0]
+    b = 2 * n
+    cnt = np.diff(starts.astype(np.int64))
+    p = pos_sorted.astype(np.float32)
+    hf = np.float32(h)
+    cell = np.floor(p / hf).astype(np.int64)
+    f = (p.astype(np.float64) - cell.astype(np.float64) * np.float64(hf)).astype(np.float32)
+    lo = np.maximum(f, 0) ** 2
+    hi = np.maximum(hf - f, 0) ** 2
+    e = [[_expand_bits(cell[:, ax] + d) << np.uint64(ax) for d in (-1, 0, 1)] for ax in range(3)]
+    span = sum(np.maximum(np.maximum(e[ax][0], e[ax][1]), e[ax][2]) - np.minimum(np.minimum(e[ax][0], e[ax][1]), e[ax][2])
+               for ax in range(3))
+    cull = span < np.uint64(b)
+    cull2 = np.float32(hf * hf) * np.float32(1.0001)
+    members = np.zeros((n, 27), np.int64)
+    k = 0
+    for a in range(3):
+        for bb in range(3):
+            for c in range(3):
+                bd2 = np.zeros(n, np.float32)
+                for ax, d in enumerate((a, bb, c)):
+                    bd2 = bd2 + (lo[:, ax] if d == 0 else (hi[:, ax] if d == 2 else np.float32(0)))
+                code = e[0][a] + e[1][bb] + e[2][c]
+                m = cnt[(code % np.uint64(b)).astype(np.int64)]
+                members[:, k] = np.where((bd2 > cull2) & cull, 0, m)
+                k += 1
+    warps = members[: n // 32 * 32].reshape(-1, 32, 27).max(1).sum(1) * 32
+    tail = members[n // 32 * 32:]
+    slots = int(warps.sum()) + (int(tail.max(0).sum()) * tail.shape[0] if tail.shape[0] else 0)
+    tree = cKDTree(p.astype(np.float64))
+    nbrs = int(tree.query_pairs(float(hf), output_type="ndarray").shape[0]) * 2
+    codes = np.stack([e[0][a] + e[1][bb] + e[2][c] for a in range(3) for bb in range(3) for c in range(3)], 1)
+    return {"candidates": int(members.sum()), "warp_slots": slots, "neighbours": nbrs, "span": span, "codes": codes}
+
+
+def host_static_neighbours(pos_sorted, span, codes, spos_ref, sstart_ref, h):
+    """Statics within h of each particle as the walk counts them: where the
+    27 Morton codes span fewer than S, each static once (the cell-filtered
+    table); elsewhere every member of the reference's buckets code % S within
+    h, so a bucket two cells share is counted twice (SF:454-490)."""
+    from scipy.spatial import cKDTree
+    s = spos_ref.shape[0]
+    p = pos_sorted.astype(np.float64)
+    q = spos_ref.astype(np.float64)
+    once = cKDTree(q).query_ball_point(p, float(h), return_length=True)
+    dup = span >= np.uint64(s)
+    total = int(once[~dup].sum())
+    h2 = float(h) ** 2
+    for i in np.nonzero(dup)[0]:
+        for code in codes[i]:
+            bkt = int(code % np.uint64(s))
+            m = q[sstart_ref[bkt]:sstart_ref[bkt + 1]]
+            if m.shape[0]:
+                total += int((((m - p[i]) ** 2).sum(1) <= h2).sum())
+    return total
+
+
+def test_neighbour_stats_match_host_count():
+    """sph_engine_neighbour_stats counts what the density walk does: the
+    candidates and the warps' candidate slots (rebuilt on the host from the
+    bucket table and the sorted positions, within 0.1 % for the rounding of
+    the skip test at its threshold), the dynamic neighbours within h and the
+    static ones (against k-d tree counts and the reference's static walk)."""
+    sc = small_scene()
+    e = SimulationEngineCUDA()
+    e.initialize(sc)
+    e.update(sc.dt, 20)
+    got = e.neighbour_stats()
+    starts, ids = e.read_buckets()
+    pos = e.read_dynamic()["pos"][ids]
+    ref = host_neighbour_stats(pos, starts, sc.params.h)
+    assert got["particles"] == sc.n
+    for key in ("candidates", "warp_slots"):
+        assert abs(got[key] - ref[key]) <= 1e-3 * ref[key], (key, got[key], ref[key])
+    assert got["warp_slots"] >= got["candidates"]
+    assert abs(got["neighbours"] - ref["neighbours"]) <= 4 + 1e-5 * ref["neighbours"], (got, ref)
+    sp, sst = e.read_static()
+    stat = host_static_neighbours(pos, ref["span"], ref["codes"], sp["pos"], sst, sc.params.h)
+    assert stat > 0
+    assert abs(got["static_neighbours"] - stat) <= 4 + 1e-5 * stat, (got, stat)
