@@ -3,7 +3,7 @@ break (FP32), through the engine's C ABI, plus the batched and served forms.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                     [--workload dam_break_1m|dam_break_16k|pool_drop_8m|batched|served]
-                    [--dt SECONDS]
+                    [--dt SECONDS] [--exact]
 
 One JSON line on stdout (rank 0).  A "step" is one SPH step of the whole
 scene: density, force/integrate, scan, scatter, gather.  The device-resident
@@ -241,6 +241,8 @@ def run_plain(args, world, rank, local, pg):
     n, s = scene.n, scene.s
     eng = SimulationEngineCUDA(local)
     eng.initialize(scene)
+    if args.exact:
+        eng.set_exact(True)
     stream = torch.cuda.ExternalStream(eng.stream_handle(), device=torch.device("cuda", local))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
@@ -319,6 +321,7 @@ def run_plain(args, world, rank, local, pg):
         "data": "synthetic (seeded SplitMix64 dam break, reference generators)",
         "config": {"workload": scene.name, "particles": n, "static_particles": s, "h": scene.params.h,
                    "dt": scene.dt, "buckets": 2 * n, "l2": "flushed (256 MiB write) before every timed step",
+                   "arithmetic": "exact (the reference's operations)" if args.exact else "fast (fused)",
                    "parallelism": "replicas" if world > 1 else "single"},
         "stage_ms": dict(zip(STAGES, [round(float(x), 5) for x in stage_ms])),
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -412,6 +415,8 @@ def main():
                     choices=["dam_break_1m", "dam_break_16k", "pool_drop_8m", "batched", "served"])
     ap.add_argument("--dt", type=float, default=None,
                     help="time step in s (default: the workload's configured 1e-4)")
+    ap.add_argument("--exact", action="store_true",
+                    help="time the reference's arithmetic (sph_engine_set_exact) instead of the fused form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the bounded batched/served samples in the default line")
@@ -422,8 +427,10 @@ def main():
         return run_reference(args)
 
     from sphfluidsimulation_gb300 import build
-    build.build()
     world, rank, local, pg = dist_setup(args)
+    if local == 0:
+        build.build()
+    barrier(pg)                      # the other ranks load what local rank 0 built
     if args.workload in ("batched", "served"):
         from sphfluidsimulation_gb300 import bench_forms
         line = bench_forms.run(args, world, rank, local, pg)

@@ -13,6 +13,7 @@ import os
 import shutil
 import subprocess
 import sys
+import tempfile
 from typing import List
 
 PKG = os.path.dirname(os.path.abspath(__file__))
@@ -60,9 +61,13 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
     os.makedirs(BUILD_DIR, exist_ok=True)
     cc = nvcc()
+    # objects and the unlinked library are private to this process, so
+    # processes building at once (ranks of one launch) never share a file;
+    # the finished library is renamed into place atomically
+    work = tempfile.mkdtemp(prefix="objs-", dir=BUILD_DIR)
 
     def compile_one(src: str) -> str:
-        obj = os.path.join(BUILD_DIR, os.path.basename(src) + ".o")
+        obj = os.path.join(work, os.path.basename(src) + ".o")
         cmd = [cc] + NVCC_FLAGS + ["-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)
@@ -72,14 +77,19 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return obj
 
     srcs = sources()
-    with cf.ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 1))) as ex:
-        objs = list(ex.map(compile_one, srcs))
-    tmp = LIB + ".tmp"
-    cmd = [cc] + ARCH + ["-shared", "-o", tmp] + objs
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
+    tmp = f"{LIB}.{os.getpid()}.tmp"
+    try:
+        with cf.ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 1))) as ex:
+            objs = list(ex.map(compile_one, srcs))
+        cmd = [cc] + ARCH + ["-shared", "-o", tmp] + objs
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, LIB)
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+        if os.path.exists(tmp):
+            os.remove(tmp)
     return LIB
 
 
