@@ -216,6 +216,21 @@ def test_update_before_initialize_is_an_error():
     with pytest.raises(SphError) as ei:
         e.update(1e-4, 1)
     assert ei.value.status == 2
+    with pytest.raises(SphError) as ei:
+        e.neighbour_stats()
+    assert ei.value.status == 2
+
+
+def test_neighbour_stats_leave_the_simulation_unchanged():
+    sc = small_scene()
+    a, b = SimulationEngineCUDA(), SimulationEngineCUDA()
+    a.initialize(sc)
+    b.initialize(sc)
+    for _ in range(3):
+        a.update(sc.dt, 4)
+        a.neighbour_stats()
+        b.update(sc.dt, 4)
+    assert a.read_dynamic_buffer().tobytes() == b.read_dynamic_buffer().tobytes()
 
 
 def test_invalid_arguments_rejected():
