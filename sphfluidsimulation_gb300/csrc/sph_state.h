@@ -195,7 +195,7 @@ private:
     // the neighbour-pass table
     sph_status enqueue_load(const float4* src, bool statics);
     sph_status enqueue_sort(int kind, bool keep_tags = false);
-    sph_status enqueue_scan(uint32_t* cnt, uint32_t* out, uint32_t len);
+    sph_status enqueue_scan(uint32_t* cnt, uint32_t* out, uint32_t len, bool cleared = false);
     sph_status alloc_arrays(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s, uint32_t cap_sq, uint32_t cap_sf,
                             uint32_t cap_sbm, uint32_t cap_t, uint32_t max_scenes, uint32_t max_tiles);
     sph_status enqueue_step_staged(bool record_accel, bool timed);

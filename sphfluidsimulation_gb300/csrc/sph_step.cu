@@ -82,10 +82,15 @@ __global__ void __launch_bounds__(kTileThreads, SPH_FORCE_MIN_CTAS) k_force(Step
 
 // Particles whose neighbour list overflowed.  A grid of a few CTAs per SM
 // walks the per-tile flags the density pass set, so a step without overflow
-// costs one flag read per tile.
+// costs one flag read per tile.  It also clears the look-back state of the
+// scan that follows it in the step (the previous scan finished long before).
 template <bool kRecord, bool kExact>
 __global__ void __launch_bounds__(kTileThreads) k_force_overflow(StepArgs a)
 {
+    const uint32_t scan_tiles = (a.scan_len + kScanTile - 1) / kScanTile;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < scan_tiles; t += gridDim.x * blockDim.x)
+        a.scan_status[t] = 0ull;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.scan_ticket = 0u;
     for (uint32_t t = blockIdx.x; t < a.num_tiles; t += gridDim.x) {
         if (a.tile_overflow[t] == 0u) continue;                  // the same for the whole CTA
         force_overflow_tile<kRecord, kExact>(a.tiles[t], a.scenes, a.pos, a.vel, a.tag, a.start,
@@ -907,11 +912,13 @@ sph_status StepState::enqueue_sort(int kind, bool keep_tags)
     return SPH_OK;
 }
 
-sph_status StepState::enqueue_scan(uint32_t* cnt, uint32_t* out, uint32_t len)
+sph_status StepState::enqueue_scan(uint32_t* cnt, uint32_t* out, uint32_t len, bool cleared)
 {
     const uint32_t tiles_n = (len + kScanTile - 1) / kScanTile;
-    CUDA_TRY(cudaMemsetAsync(scan_status, 0, sizeof(unsigned long long) * tiles_n, stream_));
-    CUDA_TRY(cudaMemsetAsync(scan_ticket, 0, sizeof(uint32_t), stream_));
+    if (!cleared) {   // the step's overflow-force kernel clears them otherwise
+        CUDA_TRY(cudaMemsetAsync(scan_status, 0, sizeof(unsigned long long) * tiles_n, stream_));
+        CUDA_TRY(cudaMemsetAsync(scan_ticket, 0, sizeof(uint32_t), stream_));
+    }
     k_scan<<<tiles_n, kScanThreads, 0, stream_>>>(cnt, out, len, scan_status, scan_ticket, err);
     CUDA_TRY(cudaGetLastError());
     return SPH_OK;
@@ -991,7 +998,7 @@ sph_status StepState::launch_step_staged(bool record_accel, bool timed)
     }
     CUDA_TRY(cudaGetLastError());
     if (timed) CUDA_TRY(cudaEventRecord(events_[2], stream_));
-    sph_status st = enqueue_scan(count, start, scan_len);
+    sph_status st = enqueue_scan(count, start, scan_len, /*cleared=*/true);
     if (st != SPH_OK) return st;
     if (timed) CUDA_TRY(cudaEventRecord(events_[3], stream_));
     k_scatter<<<nt, kTileThreads, 0, stream_>>>(s);
