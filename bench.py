@@ -304,7 +304,7 @@ def run_plain(args, world, rank, local, pg):
     t0 = time.perf_counter()
     for k in range(e2e_steps):
         eng.write_dynamic(host_in)
-        eng.update(scene.dt, 1)
+        eng.update_async(scene.dt, 1)        # the readback waits for the step
         eng.read_dynamic(host_out)
         host_in, host_out = host_out, host_in
     e2e_s = max_over_ranks(pg, time.perf_counter() - t0, local)
