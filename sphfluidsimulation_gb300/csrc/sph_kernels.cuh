@@ -960,12 +960,23 @@ __device__ __forceinline__ void force_tile(const Tile& tile, const SceneDesc* sc
             const uint32_t stride = nl.stride;
             PairSums s;
             s.fp = s.fv = s.fs = make_float3(0.f, 0.f, 0.f);
-            // four neighbours per round: eight position/velocity loads in flight
+            // four neighbours per round: eight position/velocity loads in
+            // flight.  The list entries of round r + 1 are loaded while round
+            // r's neighbours arrive, so a round waits on one load, not two.
             const uint32_t* lp = nl.nbr + i;
             uint32_t k = 0;
+            uint32_t n0 = 0, n1 = 0, n2 = 0, n3 = 0;
+            if (SPH_NBR_BATCH == 4 && k + 4 <= cd) {
+                n0 = __ldg(lp); n1 = __ldg(lp + stride); n2 = __ldg(lp + 2 * (size_t)stride);
+                n3 = __ldg(lp + 3 * (size_t)stride);
+            }
             for (; SPH_NBR_BATCH == 4 && k + 4 <= cd; k += 4, lp += 4 * (size_t)stride) {
-                const uint32_t j0 = __ldg(lp), j1 = __ldg(lp + stride), j2 = __ldg(lp + 2 * (size_t)stride),
-                               j3 = __ldg(lp + 3 * (size_t)stride);
+                const uint32_t j0 = n0, j1 = n1, j2 = n2, j3 = n3;
+                if (k + 8 <= cd) {
+                    const uint32_t* ln = lp + 4 * (size_t)stride;
+                    n0 = __ldg(ln); n1 = __ldg(ln + stride); n2 = __ldg(ln + 2 * (size_t)stride);
+                    n3 = __ldg(ln + 3 * (size_t)stride);
+                }
                 const float4 q0 = __ldg(pos + j0), q1 = __ldg(pos + j1), q2 = __ldg(pos + j2), q3 = __ldg(pos + j3);
                 const float4 u0 = __ldg(vel + j0), u1 = __ldg(vel + j1), u2 = __ldg(vel + j2), u3 = __ldg(vel + j3);
                 add_dynamic_pair<kExact>(s, p, v, pi, h, q0, u0, tag, i);
