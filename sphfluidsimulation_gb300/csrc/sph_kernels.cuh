@@ -32,7 +32,7 @@ constexpr int kTileThreads = 128;          // slots per tile = threads per CTA
 // two neighbour passes, and how many neighbours one round of the force and
 // density-sum loops loads at once.
 #ifndef SPH_DENSITY_MIN_CTAS
-#define SPH_DENSITY_MIN_CTAS 8
+#define SPH_DENSITY_MIN_CTAS 7
 #endif
 #ifndef SPH_FORCE_MIN_CTAS
 #define SPH_FORCE_MIN_CTAS 7
@@ -702,8 +702,17 @@ __device__ __forceinline__ void density_tile(uint32_t tile_index, const Tile& ti
         // four neighbours per round: their loads are issued together
         const uint32_t* lp = nl.nbr + i;
         uint32_t m = 0;
+        // the next round's entries load while this round's positions arrive
+        uint32_t n0 = 0, n1 = 0, n2 = 0, n3 = 0;
+        if (SPH_NBR_BATCH == 4 && m + 4 <= cnt) {
+            n0 = lp[0]; n1 = lp[stride]; n2 = lp[2 * (size_t)stride]; n3 = lp[3 * (size_t)stride];
+        }
         for (; SPH_NBR_BATCH == 4 && m + 4 <= cnt; m += 4, lp += 4 * (size_t)stride) {
-            const uint32_t j0 = lp[0], j1 = lp[stride], j2 = lp[2 * (size_t)stride], j3 = lp[3 * (size_t)stride];
+            const uint32_t j0 = n0, j1 = n1, j2 = n2, j3 = n3;
+            if (m + 8 <= cnt) {
+                const uint32_t* ln = lp + 4 * (size_t)stride;
+                n0 = ln[0]; n1 = ln[stride]; n2 = ln[2 * (size_t)stride]; n3 = ln[3 * (size_t)stride];
+            }
             const float4 q0 = __ldg(pos + j0), q1 = __ldg(pos + j1), q2 = __ldg(pos + j2), q3 = __ldg(pos + j3);
             sum_d = __fadd_rn(sum_d, w0_of(pair_r2<kExact>(q0, p), h));
             sum_d = __fadd_rn(sum_d, w0_of(pair_r2<kExact>(q1, p), h));
