@@ -303,9 +303,9 @@ def run_plain(args, world, rank, local, pg):
     barrier(pg)
     t0 = time.perf_counter()
     for k in range(e2e_steps):
-        eng.write_dynamic(host_in)
-        eng.update_async(scene.dt, 1)        # the readback waits for the step
-        eng.read_dynamic(host_out)
+        eng.write_dynamic_async(host_in)     # queued: upload, re-sort,
+        eng.update_async(scene.dt, 1)        # step, and the readback, which
+        eng.read_dynamic(host_out)           # waits for all of it
         host_in, host_out = host_out, host_in
     e2e_s = max_over_ranks(pg, time.perf_counter() - t0, local)
     e2e_value = world * n * e2e_steps / e2e_s

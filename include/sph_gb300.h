@@ -136,6 +136,14 @@ SPH_API sph_status sph_engine_read_dynamic_buffer(sph_engine* engine, sph_dynami
  * (input order; pressure and hash are ignored) and re-sorts. */
 SPH_API sph_status sph_engine_write_dynamic(sph_engine* engine, const sph_dynamic_particle* in);
 
+/* The same upload left queued on the engine's stream, like the OpenCL
+ * engine's LockWrite(signalEvent) / Unlock(waitEvents) pair
+ * (ParticleBufferManager.h:7-25): it returns once the work is enqueued, and
+ * `in` must stay unchanged until the next call that waits for the stream
+ * (sph_engine_synchronize, sph_engine_update, a read).  Device errors are
+ * reported by that call. */
+SPH_API sph_status sph_engine_write_dynamic_async(sph_engine* engine, const sph_dynamic_particle* in);
+
 /* GetStaticParticlesBufferManager()->LockRead(): static particles in bucket
  * order, plus the s+1 bucket-start table (may be NULL). */
 SPH_API sph_status sph_engine_read_static(sph_engine* engine, sph_static_particle* out, uint32_t* bucket_starts);

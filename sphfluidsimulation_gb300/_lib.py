@@ -69,6 +69,7 @@ _SIGS = {
     "sph_engine_read_dynamic": (_st, [_vp, _vp]),
     "sph_engine_read_dynamic_buffer": (_st, [_vp, _vp]),
     "sph_engine_write_dynamic": (_st, [_vp, _vp]),
+    "sph_engine_write_dynamic_async": (_st, [_vp, _vp]),
     "sph_engine_read_static": (_st, [_vp, _vp, _up]),
     "sph_engine_read_buckets": (_st, [_vp, _up, _up]),
     "sph_engine_simulation_time": (_st, [_vp, _dp]),

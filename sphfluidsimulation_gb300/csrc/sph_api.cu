@@ -220,6 +220,14 @@ SPH_API sph_status sph_engine_write_dynamic(sph_engine* e, const sph_dynamic_par
     return e->state.write_scene(0, in);
 }
 
+SPH_API sph_status sph_engine_write_dynamic_async(sph_engine* e, const sph_dynamic_particle* in)
+{
+    if (!e || (!in && e->n)) return SPH_ERR_INVALID_ARGUMENT;
+    if (!e->initialized) return SPH_ERR_NOT_INITIALIZED;
+    API_CUDA_TRY(cudaSetDevice(e->device));
+    return e->state.write_scene(0, in, /*wait=*/false);
+}
+
 SPH_API sph_status sph_engine_read_static(sph_engine* e, sph_static_particle* out, uint32_t* bucket_starts)
 {
     if (!e) return SPH_ERR_INVALID_ARGUMENT;

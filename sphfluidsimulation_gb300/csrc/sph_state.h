@@ -107,7 +107,9 @@ public:
     bool exact() const { return exact_; }
     // Caller's order, or with buffer_order the reference's buffer order (by tag).
     sph_status read_scene(uint32_t scene, sph_dynamic_particle* out, float* accel_out, bool buffer_order = false);
-    sph_status write_scene(uint32_t scene, const sph_dynamic_particle* in);
+    // wait = false leaves the upload and re-sort queued on the stream (the
+    // caller keeps `in` unchanged until the next synchronising call)
+    sph_status write_scene(uint32_t scene, const sph_dynamic_particle* in, bool wait = true);
     sph_status read_static(uint32_t scene, sph_static_particle* out, uint32_t* bucket_starts);
     sph_status read_buckets(uint32_t scene, uint32_t* bucket_starts, uint32_t* slot_ids);
     // particles, candidates, warp candidate slots, dynamic and static

@@ -1199,7 +1199,7 @@ sph_status StepState::read_scene(uint32_t scene, sph_dynamic_particle* out, floa
 
 // Replaces one scene's particles from host (caller's order) and re-sorts the
 // whole state (other scenes are re-sorted unchanged).
-sph_status StepState::write_scene(uint32_t scene, const sph_dynamic_particle* in)
+sph_status StepState::write_scene(uint32_t scene, const sph_dynamic_particle* in, bool wait)
 {
     if (scene >= scenes.size()) return SPH_ERR_NOT_FOUND;
     const SceneDesc& d = scenes[scene];
@@ -1216,7 +1216,7 @@ sph_status StepState::write_scene(uint32_t scene, const sph_dynamic_particle* in
     if (st != SPH_OK) return st;
     st = enqueue_sort(0, /*keep_tags=*/true);
     if (st != SPH_OK) return st;
-    return check_device_error();
+    return wait ? check_device_error() : SPH_OK;
 }
 
 sph_status StepState::read_static(uint32_t scene, sph_static_particle* out, uint32_t* bucket_starts)

@@ -130,6 +130,15 @@ class SimulationEngineCUDA:
         p = np.ascontiguousarray(particles, DYN_DTYPE)
         check(self.lib.sph_engine_write_dynamic(self.h, p.ctypes.data_as(C.c_void_p)), "sph_engine_write_dynamic")
 
+    def write_dynamic_async(self, particles: np.ndarray) -> None:
+        """Queued upload (sph_engine_write_dynamic_async): `particles` must be
+        a contiguous DYN_DTYPE array the caller keeps unchanged until the
+        next waiting call (synchronize, update, a read)."""
+        if particles.dtype != DYN_DTYPE or not particles.flags.c_contiguous:
+            raise ValueError("write_dynamic_async needs a contiguous DYN_DTYPE array (no copy is made)")
+        check(self.lib.sph_engine_write_dynamic_async(self.h, particles.ctypes.data_as(C.c_void_p)),
+              "sph_engine_write_dynamic_async")
+
     def read_static(self):
         out = np.zeros(self.s, STATIC_DTYPE)
         starts = np.zeros(self.s + 1, np.uint32)

@@ -269,6 +269,34 @@ def test_write_dynamic_round_trip_and_restart():
     assert np.sqrt(((x - y) ** 2).sum(1).mean()) <= 1e-5 * sc.params.h
 
 
+def test_queued_write_equals_waiting_write():
+    """sph_engine_write_dynamic_async followed by a queued step and a read
+    gives the bytes of the waiting upload, over several write / step / read
+    rounds from pinned host memory (the e2e loop of the benchmark)."""
+    import torch
+    from sphfluidsimulation_gb300.engine import DYN_DTYPE
+    sc = small_scene()
+    a, b = SimulationEngineCUDA(), SimulationEngineCUDA()
+    a.initialize(sc)
+    b.initialize(sc)
+    a.update(sc.dt, 3)
+    b.update(sc.dt, 3)
+    pins = [torch.empty(sc.n * 32, dtype=torch.uint8, pin_memory=True).numpy().view(DYN_DTYPE) for _ in range(2)]
+    a.read_dynamic(pins[0])
+    host = a.read_dynamic()
+    for _ in range(4):
+        a.write_dynamic_async(pins[0])
+        a.update_async(sc.dt, 2)
+        a.read_dynamic(pins[1])
+        pins.reverse()
+        b.write_dynamic(host)
+        b.update(sc.dt, 2)
+        host = b.read_dynamic()
+        assert pins[0].tobytes() == host.tobytes()
+    with pytest.raises(ValueError):
+        a.write_dynamic_async(np.zeros(sc.n, np.float32))
+
+
 def test_deterministic_repeat():
     sc = small_scene()
     out = []
