@@ -1,0 +1,3 @@
+// Test infrastructure: see BlazeEngine/AdapterShimCommon.h.
+#pragma once
+#include "BlazeEngine/AdapterShimCommon.h"
