@@ -332,8 +332,8 @@ def run_plain(args, world, rank, local, pg):
                                          float(clk.get("sm_mhz") or 0.0) if isinstance(clk, dict) else 0.0),
         "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": 32 * n,
                 "d2h_bytes_per_step": 32 * n, "steps": e2e_steps},
-        # per step: density, force, overflow force, scan, scatter, gather
-        # (the scan's two memsets are not kernels)
+        # per step: density, force, overflow force (which also clears the
+        # scan's look-back state), scan, scatter, gather
         "gpu_launches": 6 * args.steps,
         "clocks": clk,
         "wall_s_timed_region": wall,
