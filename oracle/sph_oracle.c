@@ -145,7 +145,9 @@ static inline real kernel_d2(real r, real h)
 
 /* Noise / RandomDirection (SF:140-155).  In the C++ build sin/cos/sqrt of a
  * float resolve to the double functions, and modf(double, float*) returns the
- * fractional part; the arithmetic below follows those conversions. */
+ * fractional part.  RandomDirection stores sin, cos and the square root in
+ * float variables (SF:151-153) and multiplies them in float (SF:154); the
+ * arithmetic below follows those conversions.  (The FP64 rerun keeps real.) */
 static inline float noise(float x)
 {
     double ip;
@@ -155,10 +157,10 @@ static inline vec3 random_direction(float x)
 {
     float theta = noise(x) * 2 * 3.1415f;
     float z = noise(x) * 2 - 1;
-    double s = sin((double)theta);
-    double c = cos((double)theta);
-    double z2 = sqrt((double)(1 - z * z));
-    vec3 d = { (real)(float)(z2 * c), (real)(float)(z2 * s), (real)z };
+    real s = (real)sin((double)theta);
+    real c = (real)cos((double)theta);
+    real z2 = (real)sqrt((double)(1 - z * z));
+    vec3 d = { z2 * c, z2 * s, (real)z };
     return d;
 }
 

@@ -72,6 +72,7 @@ struct StepArgs {
     const uint32_t* sbitmap;    // static-presence bitmaps of all scenes
     float4* accel;              // optional: acceleration per sorted slot (.w unused)
     uint32_t* err;              // device status word
+    uint32_t* nonfinite;        // [0] current positions, [1] positions being written
     uint32_t* bar_count;        // grid barrier (persistent kernel only)
     uint32_t* bar_gen;
     uint32_t* nbr;              // neighbour lists [k][stride]
@@ -142,18 +143,22 @@ __device__ __forceinline__ uint32_t neighbour_hash(const Neighbourhood& nb, int 
     return pick3(a, nb.ex0, nb.ex1, nb.ex2) + pick3(b, nb.ey0, nb.ey1, nb.ey2) + pick3(c, nb.ez0, nb.ez1, nb.ez2);
 }
 
-// RandomDirection (SF:140-155): sin-hash noise evaluated in double as the
-// reference's C++ build does; used only for coincident particles.
+// RandomDirection (SF:140-155), used only for coincident particles, with the
+// reference C++ build's conversions: sin of the float product in double, the
+// fraction by modf (keeping the sign of its argument, so noise lies in
+// (-1, 1) and z in (-3, 1): for z < -1 the square root is NaN, as in the
+// reference), then sin, cos and the root rounded to float and multiplied in
+// float (SF:151-154).  Every operation is rounded on its own: no contraction.
 __device__ __noinline__ inline float3 random_direction(float x)
 {
-    double s_in = (double)(x * 112.9898f);
-    double v = sin(s_in) * (double)43758.5453f;
-    float noise = (float)(v - trunc(v));
-    float theta = noise * 2.0f * 3.1415f;
-    float z = noise * 2.0f - 1.0f;
-    double sn = sin((double)theta), cs = cos((double)theta);
-    double z2 = sqrt((double)(1.0f - z * z));
-    return make_float3((float)(z2 * cs), (float)(z2 * sn), z);
+    const double v = __dmul_rn(sin((double)__fmul_rn(x, 112.9898f)), (double)43758.5453f);
+    const float noise = (float)__dsub_rn(v, trunc(v));
+    const float theta = __fmul_rn(__fmul_rn(noise, 2.0f), 3.1415f);
+    const float z = __fsub_rn(__fmul_rn(noise, 2.0f), 1.0f);
+    const float sn = (float)sin((double)theta);
+    const float cs = (float)cos((double)theta);
+    const float z2 = (float)__dsqrt_rn((double)__fsub_rn(1.0f, __fmul_rn(z, z)));
+    return make_float3(__fmul_rn(z2, cs), __fmul_rn(z2, sn), z);
 }
 
 // ClosestPointOnTriangle + CalculateTriangleForce (SF:156-223).
@@ -199,10 +204,22 @@ __device__ __noinline__ inline float3 triangle_force(float3 p, const float* tri)
 
 // ---- stage: hash + count ---------------------------------------------------
 
+// True when all three coordinates are finite.  A NaN or infinite coordinate
+// makes every distance NaN, and the reference keeps NaN distances: its tests
+// skip a neighbour only when distSqr > h^2 (SF:447-448, 488-489, 571-572,
+// 605-606) and its
+// kernels return 0 only when r >= h (SF:119-139), so a non-finite particle
+// is a neighbour of everything its buckets hold and turns their sums NaN.
+__device__ __forceinline__ bool finite3(const float4& p)
+{
+    return isfinite(p.x) && isfinite(p.y) && isfinite(p.z);
+}
+
 // key[i] = GetHash(GetCell(pos[i])) % buckets; count[q_off + key]++ with one
 // atomic per distinct key per warp; arrival[i] = rank among that key's adds.
 __device__ __forceinline__ void hash_count_tile(const Tile& tile, const SceneDesc* scenes, const float4* pos,
-                                                uint32_t* key, uint32_t* arrival, uint32_t* count)
+                                                uint32_t* key, uint32_t* arrival, uint32_t* count,
+                                                uint32_t* nonfinite = nullptr)
 {
     const SceneDesc& sc = scenes[tile.scene];
     const uint32_t i = tile.begin + threadIdx.x;
@@ -212,6 +229,7 @@ __device__ __forceinline__ void hash_count_tile(const Tile& tile, const SceneDes
         const float4 p = pos[i];
         k = fast_mod(cell_hash(p.x, p.y, p.z, sc.h), sc.fm_b);
         g = sc.q_off + k;
+        if (nonfinite && !finite3(p)) atomicOr(nonfinite, 1u);
     }
     const uint32_t r = warp_aggregated_increment(count, g, valid);
     if (valid) {
@@ -480,6 +498,7 @@ struct NbrArgs {
     uint32_t* ncount;      // dynamic count | static count << 16
     uint32_t* tile_overflow;
     uint32_t stride;
+    const uint32_t* nonfinite;   // non-zero: some current position is not finite
 };
 
 __device__ __forceinline__ float pick3f(int k, float v0, float v1, float v2)
@@ -524,7 +543,7 @@ __device__ __forceinline__ float w0_of(float r2, float h)
 {
     const float r = __fsqrt_rn(r2);
     const float w = __fsub_rn(h, r);
-    return r < h ? __fmul_rn(__fmul_rn(w, w), w) : 0.f;
+    return r >= h ? 0.f : __fmul_rn(__fmul_rn(w, w), w);   // NaN stays NaN (SF:119-125)
 }
 
 // Squared distance in the reference's own arithmetic: dir = q - p, then
@@ -568,18 +587,25 @@ struct Walk {
     bool ref_walk;      // statics walk the reference's own table (dup_s)
 };
 
+// `nonfinite_seen`: some particle of the state has a non-finite coordinate.
+// Such a particle is every visited particle's neighbour (finite3), wherever
+// its bucket lies, so cells beyond h are not skipped while one exists; and a
+// non-finite particle itself walks every bucket the reference walks: all 27
+// dynamic ones and the reference's own static table.
 template <bool kExact>
-__device__ __forceinline__ Walk make_walk(const SceneDesc& sc, const float4& p, const uint32_t* sbitmap)
+__device__ __forceinline__ Walk make_walk(const SceneDesc& sc, const float4& p, const uint32_t* sbitmap,
+                                          bool nonfinite_seen)
 {
     Walk w;
+    const bool fin = finite3(p);
     w.nb = neighbourhood(p.x, p.y, p.z, sc.h);
     w.box = cell_box(p, sc.h);
     const uint32_t span = nb_span(w.nb);
-    w.cull_d = w.box.ok && span < sc.buckets;
+    w.cull_d = w.box.ok && span < sc.buckets && !nonfinite_seen;
     w.dup_s = span >= sc.s;
     const uint32_t own = (w.nb.ex1 + w.nb.ey1 + w.nb.ez1) & sc.sbm_mask;
-    w.near_static = sc.s && ((__ldg(sbitmap + sc.sbm_off + (own >> 5)) >> (own & 31u)) & 1u);
-    w.ref_walk = w.near_static && w.dup_s;
+    w.near_static = sc.s && (!fin || ((__ldg(sbitmap + sc.sbm_off + (own >> 5)) >> (own & 31u)) & 1u));
+    w.ref_walk = w.near_static && (w.dup_s || !fin);
     return w;
 }
 
@@ -622,7 +648,7 @@ __device__ __forceinline__ void walk_neighbours_cells(const SceneDesc& sc, uint3
                     for (uint32_t j = beg; j < end; ++j) {
                         const float4 q = __ldg(pos + j);
                         const float r2 = pair_r2<kExact>(q, p);
-                        if (r2 <= h2 && j != i) on_dyn(j, q, r2);
+                        if (!(r2 > h2) && j != i) on_dyn(j, q, r2);
                     }
                     members = end > beg ? end - beg : 0u;
                 }
@@ -636,7 +662,7 @@ __device__ __forceinline__ void walk_neighbours_cells(const SceneDesc& sc, uint3
                     for (uint32_t j = sbeg; j < send; ++j) {
                         const float4 q = __ldg(st.spos_ref + j);
                         const float r2 = pair_r2<kExact>(q, p);
-                        if (r2 <= h2) on_static(j | kRefTableBit, q, r2);
+                        if (!(r2 > h2)) on_static(j | kRefTableBit, q, r2);
                     }
                 } else if (!(far && w.box.ok)) {
                     const uint32_t sb = sc.sf_off + fast_mod(hsh, sc.fm_sf);
@@ -647,7 +673,7 @@ __device__ __forceinline__ void walk_neighbours_cells(const SceneDesc& sc, uint3
                         // statics carry their cell's Morton code: only this cell's count
                         if (__float_as_uint(q.w) != hsh) continue;
                         const float r2 = pair_r2<kExact>(q, p);
-                        if (r2 <= h2) on_static(j, q, r2);
+                        if (!(r2 > h2)) on_static(j, q, r2);
                     }
                 }
             }
@@ -683,7 +709,7 @@ __device__ __forceinline__ void density_tile(uint32_t tile_index, const Tile& ti
     if (i >= tile.end) return;
     const float h = sc.h;
     const float4 p = pos[i];
-    const Walk w = make_walk<kExact>(sc, p, st.sbitmap);
+    const Walk w = make_walk<kExact>(sc, p, st.sbitmap, *nl.nonfinite != 0u);
     const uint32_t stride = nl.stride;
     uint32_t cnt = 0, scnt = 0;
     walk_neighbours<kExact>(
@@ -794,7 +820,7 @@ __device__ __forceinline__ void add_dynamic_pair(PairSums& s, const float4& p, c
     const float r2 = kExact ? __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz))
                             : __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
     const float r = __fsqrt_rn(r2);
-    if (!(r < h)) return;
+    if (r >= h) return;          // a NaN distance is kept (SF:126-139)
     if (r2 == 0.f || r == 0.f) {
         const float3 d = coincident_direction<kExact>(p, tag, i);
         dx = d.x; dy = d.y; dz = d.z;
@@ -837,7 +863,7 @@ __device__ __forceinline__ void add_static_pair(PairSums& s, const float4& p, fl
     const float r2 = kExact ? __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz))
                             : __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
     const float r = __fsqrt_rn(r2);
-    if (!(r < h)) return;
+    if (r >= h) return;          // a NaN distance is kept (SF:126-139)
     if (r2 == 0.f || r == 0.f) {
         const float3 d = coincident_direction<kExact>(p, tag, i);
         dx = d.x; dy = d.y; dz = d.z;
@@ -903,7 +929,8 @@ template <bool kRecordAccel, bool kExact>
 __device__ __forceinline__ uint32_t integrate_particle(const SceneDesc& sc, uint32_t i, const float4& p, const float4& v,
                                                        float rho, const PairSums& s, const TriangleMesh& tm,
                                                        float4* __restrict__ pos_out, float4* __restrict__ vel_out,
-                                                       uint32_t* __restrict__ key_out, float4* accel)
+                                                       uint32_t* __restrict__ key_out, float4* accel,
+                                                       uint32_t* nonfinite_next)
 {
     const float s1 = __fmul_rn(__fdiv_rn(sc.mass, __fmul_rn(2.f, rho)), sc.kc);
     const float s2 = __fmul_rn(__fmul_rn(sc.visc, sc.mass), sc.kc);
@@ -928,6 +955,7 @@ __device__ __forceinline__ uint32_t integrate_particle(const SceneDesc& sc, uint
     np.y = __fadd_rn(p.y, __fmul_rn(nv.y, sc.dt));
     np.z = __fadd_rn(p.z, __fmul_rn(nv.z, sc.dt));
     const uint32_t k = fast_mod(cell_hash(np.x, np.y, np.z, sc.h), sc.fm_b);
+    if (!(isfinite(np.x) && isfinite(np.y) && isfinite(np.z))) atomicOr(nonfinite_next, 1u);
     pos_out[i] = make_float4(np.x, np.y, np.z, p.w);
     vel_out[i] = make_float4(nv.x, nv.y, nv.z, v.w);
     key_out[i] = k;
@@ -943,6 +971,7 @@ struct ForceOut {
     uint32_t* arrival;
     uint32_t* count;
     float4* accel;
+    uint32_t* nonfinite_next;   // set when a new position is not finite
 };
 
 template <bool kRecordAccel, bool kExact>
@@ -1002,7 +1031,7 @@ __device__ __forceinline__ void force_tile(const Tile& tile, const SceneDesc* sc
             for (uint32_t k = 0; k < cs; ++k, lp += stride)
                 add_static_pair<kExact>(s, p, api, h, static_entry_pos(__ldg(lp), st), tag, i);
             g = sc.q_off + integrate_particle<kRecordAccel, kExact>(sc, i, p, v, rho, s, tm, o.pos_out, o.vel_out,
-                                                                    o.key_out, o.accel);
+                                                                    o.key_out, o.accel, o.nonfinite_next);
         }
     }
     const uint32_t r = warp_aggregated_increment(o.count, g, valid);
@@ -1032,7 +1061,7 @@ __device__ __forceinline__ void force_overflow_tile(const Tile& tile, const Scen
         const float pi = v.w;
         const float api = fabsf(pi);
         const float rho = __fadd_rn(__fdiv_rn(pi, sc.gas), sc.rho0);
-        const Walk w = make_walk<kExact>(sc, p, st.sbitmap);
+        const Walk w = make_walk<kExact>(sc, p, st.sbitmap, *nl.nonfinite != 0u);
         PairSums s;
         s.fp = s.fv = s.fs = make_float3(0.f, 0.f, 0.f);
         walk_neighbours<kExact>(
@@ -1040,7 +1069,7 @@ __device__ __forceinline__ void force_overflow_tile(const Tile& tile, const Scen
             [&](uint32_t j, const float4& q, float) { add_dynamic_pair<kExact>(s, p, v, pi, h, q, __ldg(vel + j), tag, i); },
             [&](uint32_t, const float4& q, float) { add_static_pair<kExact>(s, p, api, h, q, tag, i); });
         g = sc.q_off + integrate_particle<kRecordAccel, kExact>(sc, i, p, v, rho, s, tm, o.pos_out, o.vel_out,
-                                                                o.key_out, o.accel);
+                                                                o.key_out, o.accel, o.nonfinite_next);
     }
     const uint32_t r = warp_aggregated_increment(o.count, g, valid);
     if (valid) o.arrival[i] = r;

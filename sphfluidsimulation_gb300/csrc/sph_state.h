@@ -31,6 +31,8 @@ struct SortArgs {
     uint32_t* count;
     uint32_t* start;
     uint32_t* err;
+    uint32_t* nonfinite_set;     // hash + count marks a non-finite position here (or null)
+    uint32_t* nonfinite_rotate;  // the step's gather moves [1] to [0] and clears [1] (or null)
 };
 
 // One scene as the caller hands it over (host pointers, caller's order).
@@ -174,6 +176,9 @@ public:
     uint32_t* scan_ticket = nullptr;
     uint32_t* err = nullptr;
     uint32_t* bar = nullptr;
+    // [0]: some current position is not finite (read by the walks);
+    // [1]: the same for the positions the force pass is writing
+    uint32_t* nonfinite = nullptr;
     float4* spos = nullptr;        // statics sorted by the neighbour-pass table
     uint32_t* sstart = nullptr;
     float4* spos_ref = nullptr;    // statics sorted by the reference's s-bucket table
@@ -226,6 +231,7 @@ private:
     float4* saved_vel_ = nullptr;
     uint32_t* saved_start_ = nullptr;
     uint32_t* saved_tag_ = nullptr;
+    uint32_t saved_nonfinite_[2] = {0u, 0u};
     uint32_t* err_host_ = nullptr;                // pinned copy of the status word
     unsigned long long* render_zkey_ = nullptr;   // render targets, kept between frames
     uchar4* render_rgba_ = nullptr;

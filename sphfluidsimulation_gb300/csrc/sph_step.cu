@@ -23,7 +23,7 @@ namespace sph {
 
 __global__ void __launch_bounds__(kTileThreads) k_hash_count(SortArgs a)
 {
-    hash_count_tile(a.tiles[blockIdx.x], a.scenes, a.pos_src, a.key, a.arrival, a.count);
+    hash_count_tile(a.tiles[blockIdx.x], a.scenes, a.pos_src, a.key, a.arrival, a.count, a.nonfinite_set);
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan(uint32_t* count, uint32_t* start, uint32_t len,
@@ -44,11 +44,15 @@ __global__ void __launch_bounds__(kTileThreads) k_gather(SortArgs a)
 {
     gather_tile(a.tiles[blockIdx.x], a.scenes, a.key, a.arrival, a.ptag, a.start, a.pos_src, a.vel_src,
                 a.pos_dst, a.vel_dst, a.tag_dst, a.assign, a.err, a.accel_src, a.accel_dst);
+    if (a.nonfinite_rotate && blockIdx.x == 0 && threadIdx.x == 0) {   // the force pass has finished
+        a.nonfinite_rotate[0] = a.nonfinite_rotate[1];
+        a.nonfinite_rotate[1] = 0u;
+    }
 }
 
 __device__ __forceinline__ NbrArgs nbr_args(const StepArgs& a)
 {
-    return NbrArgs{a.nbr, a.snbr, a.ncount, a.tile_overflow, a.nbr_stride};
+    return NbrArgs{a.nbr, a.snbr, a.ncount, a.tile_overflow, a.nbr_stride, a.nonfinite};
 }
 
 __device__ __forceinline__ StaticTables static_tables(const StepArgs& a)
@@ -63,7 +67,7 @@ __device__ __forceinline__ TriangleMesh triangle_mesh(const StepArgs& a)
 
 __device__ __forceinline__ ForceOut force_out(const StepArgs& a)
 {
-    return ForceOut{a.pos_tmp, a.vel_tmp, a.key, a.arrival, a.count, a.accel};
+    return ForceOut{a.pos_tmp, a.vel_tmp, a.key, a.arrival, a.count, a.accel, a.nonfinite + 1};
 }
 
 template <bool kExact>
@@ -116,7 +120,7 @@ __global__ void __launch_bounds__(kTileThreads) k_neighbour_stats(StepArgs a, un
     unsigned long long v[5] = {valid ? 1ull : 0ull, 0ull, 0ull, 0ull, 0ull};
     if (valid) {
         const float4 p = a.pos[i];
-        const Walk w = make_walk<false>(sc, p, a.sbitmap);
+        const Walk w = make_walk<false>(sc, p, a.sbitmap, a.nonfinite[0] != 0u);
         walk_neighbours_cells<false>(
             sc, i, p, w, a.pos, a.start, static_tables(a),
             [&](uint32_t, const float4&, float) { ++v[3]; },
@@ -186,6 +190,10 @@ __global__ void __launch_bounds__(kTileThreads) k_step_persistent(StepArgs a, ui
         }
     }
     grid_barrier(a.bar_count, a.bar_gen, a.err);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {   // every walk of this step has read [0]
+        a.nonfinite[0] = a.nonfinite[1];
+        a.nonfinite[1] = 0u;
+    }
     for (uint32_t t = blockIdx.x; t < scan_tiles; t += gridDim.x)
         scan_tile(t, a.count, a.start, a.scan_len, a.scan_status, a.err, sm);
     grid_barrier(a.bar_count, a.bar_gen, a.err);
@@ -303,7 +311,8 @@ void StepState::release()
 {
     if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
     void* ptrs[] = {d_scenes, d_sscenes, d_sfscenes, d_tiles, d_stiles, pos, vel, pos_tmp, vel_tmp, key, arrival,
-                    ptag, count, start, scan_status, scan_ticket, err, bar, spos, sstart, spos_ref, sstart_ref, tris,
+                    ptag, count, start, scan_status, scan_ticket, err, bar, nonfinite, spos, sstart, spos_ref,
+                    sstart_ref, tris,
                     accel, accel_tmp, accel_io, staging, d_tmp_tiles_, d_tmp_scene_, nbr, snbr, ncount, tile_overflow,
                     saved_pos_, saved_vel_, saved_start_, sbitmap, tag, tag_io, saved_tag_, tri_cells, tri_list,
                     render_zkey_, render_rgba_, render_depth_};
@@ -325,7 +334,7 @@ void StepState::release()
     d_tiles = d_stiles = d_tmp_tiles_ = nullptr;
     pos = vel = pos_tmp = vel_tmp = spos = accel = accel_tmp = accel_io = nullptr;
     staging = nullptr;
-    key = arrival = ptag = count = start = scan_ticket = err = bar = sstart = nullptr;
+    key = arrival = ptag = count = start = scan_ticket = err = bar = nonfinite = sstart = nullptr;
     scan_status = nullptr;
     tris = nullptr;
     for (auto& e : events_)
@@ -535,6 +544,7 @@ sph_status StepState::alloc_arrays(uint32_t cap_n, uint32_t cap_q, uint32_t cap_
     ALLOC(scan_ticket, 1);
     ALLOC(err, 1);
     ALLOC(bar, 2);
+    ALLOC(nonfinite, 2);
     ALLOC(spos, cap_s);
     ALLOC(sstart, cap_sf + 1ull);
     ALLOC(spos_ref, cap_s);
@@ -550,6 +560,7 @@ sph_status StepState::alloc_arrays(uint32_t cap_n, uint32_t cap_q, uint32_t cap_
     CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(uint32_t) * cnt_len, stream_));
     CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(uint32_t), stream_));
     CUDA_TRY(cudaMemsetAsync(bar, 0, 2 * sizeof(uint32_t), stream_));
+    CUDA_TRY(cudaMemsetAsync(nonfinite, 0, 2 * sizeof(uint32_t), stream_));
     CUDA_TRY(cudaMemsetAsync(scan_status, 0, sizeof(unsigned long long) * scan_tiles_max, stream_));
     CUDA_TRY(cudaMemsetAsync(tile_overflow, 0, sizeof(uint32_t) * max_tiles_, stream_));
     CUDA_TRY(cudaMemsetAsync(sbitmap, 0, sizeof(uint32_t) * std::max<uint32_t>(cap_sbm, 1), stream_));
@@ -884,6 +895,8 @@ SortArgs StepState::sort_args(int kind) const
     a.count = count;
     a.start = kind == 0 ? start : (kind == 1 ? sstart_ref : sstart);
     a.err = err;
+    a.nonfinite_set = kind == 0 ? nonfinite : nullptr;   // dynamic sorts mark the current word
+    a.nonfinite_rotate = nullptr;
     return a;
 }
 
@@ -953,6 +966,7 @@ StepArgs StepState::step_args() const
     a.sbitmap = sbitmap;
     a.accel = accel_tmp;
     a.err = err;
+    a.nonfinite = nonfinite;
     a.bar_count = bar;
     a.bar_gen = bar + 1;
     a.nbr = nbr;
@@ -981,6 +995,8 @@ sph_status StepState::launch_step_staged(bool record_accel, bool timed)
     s.tag_src = tag;          // the step's sort: tags per scene reorder flag
     s.tag_dst = tag;
     s.assign = kTagStep;
+    s.nonfinite_set = nullptr;       // keys come from the force pass
+    s.nonfinite_rotate = nonfinite;
     if (record_accel) {       // the recorded acceleration follows its particle
         s.accel_src = accel_tmp;
         s.accel_dst = accel;
@@ -1214,6 +1230,8 @@ sph_status StepState::write_scene(uint32_t scene, const sph_dynamic_particle* in
     CUDA_TRY(cudaMemcpyAsync(staging + 2ull * d.p_off, in, sizeof(sph_dynamic_particle) * d.n, cudaMemcpyHostToDevice, stream_));
     sph_status st = enqueue_load(staging, false);
     if (st != SPH_OK) return st;
+    // the re-sort hashes every particle again: it recomputes the flag
+    CUDA_TRY(cudaMemsetAsync(nonfinite, 0, 2 * sizeof(uint32_t), stream_));
     st = enqueue_sort(0, /*keep_tags=*/true);
     if (st != SPH_OK) return st;
     return wait ? check_device_error() : SPH_OK;
@@ -1315,6 +1333,7 @@ sph_status StepState::save_state()
     CUDA_TRY(cudaMemcpyAsync(saved_pos_, pos, sizeof(float4) * cap_n_, cudaMemcpyDeviceToDevice, stream_));
     CUDA_TRY(cudaMemcpyAsync(saved_vel_, vel, sizeof(float4) * cap_n_, cudaMemcpyDeviceToDevice, stream_));
     CUDA_TRY(cudaMemcpyAsync(saved_start_, start, sizeof(uint32_t) * (cap_q_ + 1ull), cudaMemcpyDeviceToDevice, stream_));
+    CUDA_TRY(cudaMemcpyAsync(saved_nonfinite_, nonfinite, sizeof saved_nonfinite_, cudaMemcpyDeviceToHost, stream_));
     CUDA_TRY(cudaStreamSynchronize(stream_));
     return SPH_OK;
 }
@@ -1326,6 +1345,7 @@ sph_status StepState::restore_state()
     CUDA_TRY(cudaMemcpyAsync(pos, saved_pos_, sizeof(float4) * cap_n_, cudaMemcpyDeviceToDevice, stream_));
     CUDA_TRY(cudaMemcpyAsync(vel, saved_vel_, sizeof(float4) * cap_n_, cudaMemcpyDeviceToDevice, stream_));
     CUDA_TRY(cudaMemcpyAsync(start, saved_start_, sizeof(uint32_t) * (cap_q_ + 1ull), cudaMemcpyDeviceToDevice, stream_));
+    CUDA_TRY(cudaMemcpyAsync(nonfinite, saved_nonfinite_, sizeof saved_nonfinite_, cudaMemcpyHostToDevice, stream_));
     CUDA_TRY(cudaStreamSynchronize(stream_));
     return SPH_OK;
 }

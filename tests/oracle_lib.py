@@ -233,6 +233,9 @@ class RefEngine:
 
     def update(self, dt: float, steps: int) -> None:
         assert self.L.sph_ref_update(self.h, float(dt), int(steps)) == 0
+        # the reference prints warnings with C stdio (coincident particles);
+        # flush them while the caller's output capture is still in place
+        C.CDLL(None).fflush(None)
 
     def read_raw(self) -> np.ndarray:
         out = np.zeros(self.n, DYN_DTYPE)
@@ -280,3 +283,34 @@ def oracle_splat(proj, view, model, width: int, height: int, dyn4, dyn_layer, st
     assert rc == 0
     return rgba, depth
 
+
+
+def coincident_scene():
+    """A walled dam break (4,800 particles) plus 64 exact duplicates of fluid
+    particles and 8 fluid particles placed exactly on floor wall particles:
+    every coincident pair takes RandomDirection (SPHFunctions.cpp:140-155)
+    in the force pass, against a dynamic (SF:576-580) or a static
+    (SF:610-614) neighbour."""
+    from sphfluidsimulation_gb300 import scenes
+    base = scenes.dam_break((20, 12, 20), 0.02, 0.04, (0.6, 0.4, 0.6), 0, mass=0.008, name="dam_4800")
+    rng = np.random.default_rng(7)
+    dup = base.dyn_pos[rng.choice(base.n, 64, replace=False)]
+    w = base.static_pos
+    floor = w[(w[:, 1] == 0.0) & (w[:, 0] > 0.1) & (w[:, 0] < 0.3) & (w[:, 2] > 0.1) & (w[:, 2] < 0.3)]
+    on_wall = floor[rng.choice(floor.shape[0], 8, replace=False)]
+    pos = np.concatenate([base.dyn_pos, dup, on_wall], 0).astype(np.float32)
+    return scenes.Scene(name="coincident", dyn_pos=pos, static_pos=w, params=base.params, dt=base.dt, steps=0)
+
+
+def differing_words(a, b) -> np.ndarray:
+    """(n, 8) mask of the 32-bit words in which two particle buffers (the
+    reference's 32-byte DynamicParticle records) differ, where any NaN equals
+    any NaN in the seven float fields: the sign and payload of a NaN depend
+    on the platform that produced it.  The hash field is compared as an
+    integer."""
+    ua = np.asarray(a).view(np.uint32).reshape(-1, 8)
+    ub = np.asarray(b).view(np.uint32).reshape(-1, 8)
+    diff = ua != ub
+    both_nan = np.isnan(ua[:, :7].view(np.float32)) & np.isnan(ub[:, :7].view(np.float32))
+    diff[:, :7] &= ~both_nan
+    return diff

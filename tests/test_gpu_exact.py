@@ -22,7 +22,7 @@ import os
 import numpy as np
 import pytest
 
-from oracle_lib import Oracle
+from oracle_lib import Oracle, coincident_scene, differing_words
 from sphfluidsimulation_gb300 import scenes
 from sphfluidsimulation_gb300.engine import SimulationEngineCUDA
 
@@ -245,3 +245,26 @@ def test_pool_drop_8m_exact_and_default_arithmetic():
     n, b = sc.n, 2 * sc.n
     assert starts[0] == 0 and starts[b] == n and (np.diff(starts.astype(np.int64)) >= 0).all()
     assert np.array_equal(np.sort(ids), np.arange(n, dtype=np.uint32))
+
+
+def test_exact_coincident_particles():
+    """Particles at exactly the same position as a dynamic or a static
+    neighbour take the reference's RandomDirection (SF:140-155, used at
+    SF:576-580 and SF:610-614): sin and cos in double, rounded to float.
+    For about half of the seeds the reference's noise is negative (modf keeps
+    the sign), z falls below -1 and the direction is NaN, so those particles
+    turn NaN, and NaN spreads to their neighbours.  Over three steps every
+    finite word equals the oracle's and the NaNs sit in the same words (their
+    sign and payload are the platform's).  The device's and the host's double
+    sin and cos may differ in the last bit, which reaches the float result
+    only within about 1e-12 of a float rounding boundary."""
+    sc = coincident_scene()
+    o = Oracle(0)
+    o.init(sc)
+    e = exact_engine(sc)
+    for step in range(1, 4):
+        o.update(sc.dt, 1)
+        e.update(sc.dt, 1)
+        diff = differing_words(e.read_dynamic_buffer(), o.read_raw())
+        assert not diff.any(), f"after {step} steps: {int(diff.any(1).sum())} particles differ, per field {diff.sum(0)}"
+    assert np.isnan(o.read_raw()["pos"]).any()

@@ -7,7 +7,7 @@ import os
 import numpy as np
 import pytest
 
-from oracle_lib import REF_SO, Oracle, RefEngine, oracle_counting_sort, oracle_hash
+from oracle_lib import REF_SO, Oracle, RefEngine, coincident_scene, differing_words, oracle_counting_sort, oracle_hash
 from sphfluidsimulation_gb300 import scenes
 
 GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
@@ -161,6 +161,27 @@ def test_oracle_matches_reference_random_scene():
         r.update(sc.dt, steps)
         assert o.read_raw().tobytes() == r.read_raw().tobytes()
         assert all(np.array_equal(x, y) for x, y in zip(o.maps(), r.maps()))
+
+
+@pytest.mark.skipif(not os.path.exists(REF_SO), reason="reference not compiled here (no reference tree)")
+def test_oracle_matches_reference_coincident_particles():
+    """RandomDirection (SF:140-155) for coincident dynamic and static pairs:
+    the oracle's restatement gives the reference's own bytes.  About half of
+    the seeds make the reference's noise negative (modf keeps the sign), z
+    then falls below -1 and the direction is NaN; those particles turn NaN
+    in both, and NaN spreads to their neighbours in later steps."""
+    sc = coincident_scene()
+    o, r = Oracle(0), RefEngine()
+    o.init(sc)
+    r.init(sc)
+    o.update(sc.dt, 1)
+    r.update(sc.dt, 1)
+    assert o.read_raw().tobytes() == r.read_raw().tobytes()       # same NaN bits too, at first
+    assert np.isnan(o.read_raw()["pos"]).any()
+    for steps in (1, 2):
+        o.update(sc.dt, steps)
+        r.update(sc.dt, steps)
+        assert not differing_words(o.read_raw(), r.read_raw()).any()
 
 
 def test_reorder_cadence_and_identity():
