@@ -314,3 +314,43 @@ def differing_words(a, b) -> np.ndarray:
     both_nan = np.isnan(ua[:, :7].view(np.float32)) & np.isnan(ub[:, :7].view(np.float32))
     diff[:, :7] &= ~both_nan
     return diff
+
+
+def random_scene(seed: int):
+    """A seeded random scene for exact-arithmetic fuzzing: h from 0.02 to 1,
+    50-4000 particles as a uniform cloud, Gaussian clusters, a thin sheet or
+    a lattice at h/2 placed on cell faces (+-1e-6); walls (a BoxShell at h/2
+    around them) on 60 % of seeds; random mass, gas constant, viscosity,
+    gravity direction, rest density, dt, reorder mode and initial
+    velocities.  Returns (scene, velocities or None)."""
+    from sphfluidsimulation_gb300 import scenes
+    rng = np.random.default_rng(seed)
+    h = float(rng.choice([0.02, 0.05, 0.1, 0.3, 1.0]))
+    n = int(rng.integers(50, 4000))
+    kind = rng.integers(0, 4)
+    if kind == 0:
+        pos = rng.uniform(-3 * h * n ** (1 / 3) / 4, 3 * h * n ** (1 / 3) / 4, size=(n, 3))
+    elif kind == 1:
+        c = rng.uniform(-5 * h, 5 * h, size=(5, 3))
+        pos = c[rng.integers(0, 5, n)] + rng.normal(0, h * 0.7, size=(n, 3))
+    elif kind == 2:
+        pos = np.stack([rng.uniform(0, 20 * h, n), rng.uniform(0, 0.3 * h, n), rng.uniform(0, 20 * h, n)], 1)
+    else:
+        m = int(round(n ** (1 / 3))) + 1
+        g = np.stack(np.meshgrid(*[np.arange(m)] * 3, indexing="ij"), -1).reshape(-1, 3)[:n]
+        pos = g * (h / 2) + rng.uniform(-1e-6, 1e-6, size=g.shape)
+    pos = pos.astype(np.float32)
+    walls = np.zeros((0, 3), np.float32)
+    if rng.random() < 0.6:
+        lo, hi = pos.min(0) - h * 0.3, pos.max(0) + h * 0.3
+        walls = scenes.box_shell(hi - lo, h / 2, offset=lo).astype(np.float32)
+    params = scenes.Params(particle_mass=float(rng.uniform(0.001, 2.0)),
+                           gas_constant=float(rng.choice([50.0, 200.0, 2000.0])), elasticity=0.0,
+                           viscosity=float(rng.choice([0.0, 0.1, 1.0])),
+                           gravity=tuple(float(v) for v in rng.normal(0, 5, 3)),
+                           rest_density=float(rng.choice([100.0, 1000.0])), h=h)
+    interval = float(rng.choice([np.finfo(np.float32).max, -1.0]))
+    vel = rng.normal(0, 0.5, size=(n, 3)).astype(np.float32) if rng.random() < 0.5 else None
+    sc = scenes.Scene(name=f"random_{seed}", dyn_pos=pos, static_pos=walls, params=params,
+                      dt=float(rng.choice([1e-4, 1e-3])), steps=0, reorder_interval=interval)
+    return sc, vel

@@ -106,3 +106,40 @@ def test_batch_exact_arithmetic_equals_the_oracle():
             ref = np.empty(sc.n, o.read_raw().dtype)
             ref[io] = o.read_raw()
             assert b.read_scene(sid).tobytes() == ref.tobytes(), (mode, sc.name)
+
+
+def test_batch_of_random_scenes_equals_the_oracle():
+    """Six seeded random scenes (tests/oracle_lib.random_scene) of different
+    smoothing radii, sizes, walls, constants and time steps in one batch:
+    with the reference's arithmetic each reproduces the oracle's bytes, in
+    both batch modes.  Batches do not reorder, so the oracle runs map mode."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(__file__))
+    from oracle_lib import Oracle, differing_words, random_scene
+    scs = []
+    for seed in range(200, 206):
+        sc, vel = random_scene(seed)
+        sc.dyn_vel = vel
+        sc.reorder_interval = float(np.finfo(np.float32).max)
+        scs.append(sc)
+    refs = []
+    for sc in scs:
+        o = Oracle(0)
+        o.init(sc, sc.dyn_vel)
+        o.update(sc.dt, 5)
+        _, _, io = o.maps()
+        ref = np.empty(sc.n, o.read_raw().dtype)
+        ref[io] = o.read_raw()
+        refs.append(ref)
+    for mode in (0, 1):
+        b = Batch()
+        ids = [b.add_scene(sc) for sc in scs]
+        b.finalize()
+        b.set_mode(mode)
+        b.set_exact(True)
+        b.step(2)
+        b.step(3)
+        for sid, sc, ref in zip(ids, scs, refs):
+            diff = differing_words(b.read_scene(sid), ref)
+            assert not diff.any(), (mode, sc.name, int(diff.any(1).sum()))

@@ -22,7 +22,7 @@ import os
 import numpy as np
 import pytest
 
-from oracle_lib import Oracle, coincident_scene, differing_words
+from oracle_lib import Oracle, coincident_scene, differing_words, random_scene
 from sphfluidsimulation_gb300 import scenes
 from sphfluidsimulation_gb300.engine import SimulationEngineCUDA
 
@@ -268,3 +268,22 @@ def test_exact_coincident_particles():
         diff = differing_words(e.read_dynamic_buffer(), o.read_raw())
         assert not diff.any(), f"after {step} steps: {int(diff.any(1).sum())} particles differ, per field {diff.sum(0)}"
     assert np.isnan(o.read_raw()["pos"]).any()
+
+
+@pytest.mark.parametrize("seed", range(100, 116))
+def test_exact_random_scenes(seed):
+    """Seeded random scenes (tests/oracle_lib.random_scene): clouds,
+    clusters, sheets and face-aligned lattices, with and without walls,
+    random constants, gravity, dt, reorder mode and initial velocities.
+    Six exact steps equal the oracle's bytes."""
+    sc, vel = random_scene(seed)
+    o = Oracle(0)
+    o.init(sc, vel)
+    e = SimulationEngineCUDA()
+    e.initialize(sc, vel)
+    e.set_exact(True)
+    for steps in (1, 2, 3):
+        o.update(sc.dt, steps)
+        e.update(sc.dt, steps)
+        diff = differing_words(e.read_dynamic_buffer(), o.read_raw())
+        assert not diff.any(), f"{sc.name}: {int(diff.any(1).sum())} particles differ, per field {diff.sum(0)}"
