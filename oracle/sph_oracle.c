@@ -80,14 +80,19 @@ typedef struct { real x, y, z; } vec3;
 
 /* ---- hash (SF:65-114) -------------------------------------------------- */
 
-/* Floor(): the OpenCL side reinterprets the int result of floor as uint
- * (SF:67-68, as_uint3(convert_int3_rtn)). The C++ side casts float->uint
- * directly (SF:70-74), which is undefined for negative values; on x86-64 g++
- * it yields the same wrapped value.  The int->uint reinterpretation is used
- * here so negative cells behave the same on every host. */
+/* Floor(): the C++ engine casts floor(v) from float to uint directly
+ * (SF:70-74), which C++ leaves undefined for negative and out-of-range
+ * values.  x86-64 g++ compiles the cast as a conversion to int64 followed by
+ * truncation to 32 bits: cells wrap modulo 2^32 for every |v| < 2^63, and
+ * NaN, the infinities and larger values give the conversion's "indefinite"
+ * 0x8000000000000000, whose low 32 bits are 0.  Those steps are written out
+ * here, so every host (x86-64 and aarch64 alike) produces the same bits.
+ * (The OpenCL side converts to int first, SF:67-68, which agrees for
+ * |v| < 2^31.) */
 static inline uint32_t floor_to_cell(real v)
 {
-    return (uint32_t)(int32_t)RFLOOR(v);
+    const real f = RFLOOR(v);
+    return (f >= (real)-9223372036854775808.0 && f < (real)9223372036854775808.0) ? (uint32_t)(int64_t)f : 0u;
 }
 
 /* ExpandBits (SF:78-86): spread the low 10 bits of v to every third bit. */

@@ -75,12 +75,16 @@ SPH_HD uint32_t expand_bits(uint32_t v)
     return v;
 }
 
-// Floor (SF:65-76): floor of position / h reinterpreted as unsigned, so
-// negative cells wrap (the OpenCL semantics; x86-64 g++ produces the same
-// for the C++ path).  x / h is an IEEE division: never built with fast math.
+// Floor (SF:65-76): the C++ engine casts floorf(position / h) to uint32.
+// x86-64 g++ converts through int64 and keeps the low 32 bits, so cells wrap
+// modulo 2^32 for every |value| < 2^63 (negative ones included); NaN, the
+// infinities and larger values give int64's "indefinite" 0x8000000000000000,
+// whose low bits are 0.  Written out here, so every host and the device give
+// those bits.  x / h is an IEEE division: never built with fast math.
 SPH_HD uint32_t cell_coord(float x, float h)
 {
-    return (uint32_t)(int32_t)floorf(x / h);
+    const float f = floorf(x / h);
+    return (f >= -9223372036854775808.f && f < 9223372036854775808.f) ? (uint32_t)(int64_t)f : 0u;
 }
 
 // Morton3D (SF:88-97) of a cell: x in bit 0, y in bit 1, z in bit 2.

@@ -523,9 +523,10 @@ struct CellBox {
 __device__ __forceinline__ CellBox cell_box(const float4& p, float h)
 {
     CellBox b;
-    const int32_t cx = (int32_t)cell_coord(p.x, h), cy = (int32_t)cell_coord(p.y, h), cz = (int32_t)cell_coord(p.z, h);
-    b.ok = abs(cx) < (1 << 22) && abs(cy) < (1 << 22) && abs(cz) < (1 << 22);
-    const float fx = p.x - (float)cx * h, fy = p.y - (float)cy * h, fz = p.z - (float)cz * h;
+    // the unwrapped cell, exact as a float while |cell| < 2^22 (NaN: not ok)
+    const float cx = floorf(p.x / h), cy = floorf(p.y / h), cz = floorf(p.z / h);
+    b.ok = fabsf(cx) < 4194304.f && fabsf(cy) < 4194304.f && fabsf(cz) < 4194304.f;
+    const float fx = p.x - cx * h, fy = p.y - cy * h, fz = p.z - cz * h;
     const float gx = fmaxf(h - fx, 0.f), gy = fmaxf(h - fy, 0.f), gz = fmaxf(h - fz, 0.f);
     const float ax = fmaxf(fx, 0.f), ay = fmaxf(fy, 0.f), az = fmaxf(fz, 0.f);
     b.x0 = ax * ax; b.x2 = gx * gx;

@@ -102,3 +102,18 @@ def test_sort_one_million_properties():
     # inside each bucket the input indices descend, as the reference's fill leaves them
     same = np.diff(k_sorted.astype(np.int64)) == 0
     assert (np.diff(order.astype(np.int64))[same] < 0).all()
+
+
+def test_sort_far_cells_and_non_finite():
+    """Cells far beyond the 10-bit Morton range: the reference's float->uint
+    cast wraps modulo 2^32 (through int64 on x86-64) up to 2^63 cells, on both
+    sides, and NaN maps to cell 0.  Keys, counts, starts and slot order equal
+    the oracle's."""
+    rng = np.random.default_rng(11)
+    h = 0.04
+    mags = np.float32(10.0) ** rng.uniform(0, 17, size=(4000, 3)).astype(np.float32)
+    signs = np.where(rng.random((4000, 3)) < 0.5, -1.0, 1.0).astype(np.float32)
+    pos = (mags * signs * np.float32(h)).astype(np.float32)
+    pos[::97, 1] = np.nan
+    pos[::131, 0] = np.inf
+    check_sort(pos, h, 8000)

@@ -184,6 +184,29 @@ def test_oracle_matches_reference_coincident_particles():
         assert not differing_words(o.read_raw(), r.read_raw()).any()
 
 
+@pytest.mark.skipif(not os.path.exists(REF_SO), reason="reference not compiled here (no reference tree)")
+def test_oracle_matches_reference_far_cells():
+    """Cells beyond 2^31 (SF:65-76 casts floor(p/h) from float to uint): the
+    reference's cast wraps modulo 2^32 through int64 on x86-64, and the
+    oracle writes those two steps out; beyond 2^63 cells and for the
+    infinities the conversion's "indefinite" value leaves cell 0.  Particles
+    up to 2^66 cells away, on both sides, and infinite ones hash and step to
+    the reference's bytes."""
+    sc = scenes.dam_break((6, 5, 7), 0.02, 0.04, (0.3, 0.3, 0.3), 0, mass=0.008)
+    far = np.array([[3.0e9, 0.1, 0.1], [-5.0e9, 0.2, 0.3], [1.0e12, -2.5e11, 0.1], [2.0e17, 0.3, -7.0e16],
+                    [0.1, 4.1e9, 0.2], [0.2, 0.2, -2.2e9], [4.5e16, 4.5e16, 4.5e16], [1.0e20, 0.1, 0.1],
+                    [0.1, -3.0e19, 0.2], [np.inf, 0.1, 0.1], [0.2, -np.inf, 0.2]], np.float32) * np.float32(0.04)
+    sc.dyn_pos = np.concatenate([sc.dyn_pos, far], 0).astype(np.float32)
+    o, r = Oracle(0), RefEngine()
+    o.init(sc)
+    r.init(sc)
+    assert o.read_raw().tobytes() == r.read_raw().tobytes()
+    o.update(sc.dt, 2)
+    r.update(sc.dt, 2)
+    assert o.read_raw().tobytes() == r.read_raw().tobytes()
+    assert all(np.array_equal(x, y) for x, y in zip(o.maps(), r.maps()))
+
+
 def test_reorder_cadence_and_identity():
     """reorderTimeInterval: a negative interval reorders on every Update call,
     any interval >= 0 never does (the elapsed time is reset as soon as it
