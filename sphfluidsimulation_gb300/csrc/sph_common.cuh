@@ -135,7 +135,7 @@ struct SceneDesc {
 };
 
 // Reach of a boundary triangle: CalculateTriangleForce returns zero beyond
-// this distance (SF:206, 214-215).
+// this distance (SF:209, 219-220).
 constexpr float kTriangleReach = 2.5f;
 
 // A tile: up to one CTA's worth of consecutive slots of one scene.

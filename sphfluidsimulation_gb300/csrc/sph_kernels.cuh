@@ -911,7 +911,9 @@ __device__ __forceinline__ void add_triangle_forces(const SceneDesc& sc, const T
         const float3 tf = triangle_force(p, tm.tris + 9u * t);
         f.x = __fadd_rn(f.x, tf.x); f.y = __fadd_rn(f.y, tf.y); f.z = __fadd_rn(f.z, tf.z);
     };
-    if (sc.tg_nx == 0) {
+    // no grid, or a non-finite particle: every triangle, as the reference
+    // evaluates them (each returns NaN for a NaN distance, SF:219-220)
+    if (sc.tg_nx == 0 || !(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) {
         for (uint32_t t = 0; t < sc.t; ++t) add(sc.t_off + t);
         return;
     }
