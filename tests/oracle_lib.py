@@ -354,3 +354,22 @@ def random_scene(seed: int):
     sc = scenes.Scene(name=f"random_{seed}", dyn_pos=pos, static_pos=walls, params=params,
                       dt=float(rng.choice([1e-4, 1e-3])), steps=0, reorder_interval=interval)
     return sc, vel
+
+
+def triangle_soup_scene(seed: int):
+    """A 600-particle block (h = 0.5) among 40 random triangles, some of them
+    degenerate (two equal vertices, three collinear ones, a tiny one), and
+    one particle exactly on a triangle's vertex: CalculateTriangleForce
+    (SPHFunctions.cpp:207-223) at and near its divisions by zero."""
+    from sphfluidsimulation_gb300 import scenes
+    rng = np.random.default_rng(seed)
+    h = 0.5
+    dyn = scenes.filled_box((10, 6, 10), 0.25, (1.0, 1.0, 1.0), 0.1, scenes.SplitMix64(seed))
+    tris = rng.uniform(0.0, 5.0, size=(40, 9)).astype(np.float32)
+    tris[0, 3:6] = tris[0, 0:3]                                   # two equal vertices
+    tris[1, 3:6] = tris[1, 0:3] + np.float32(0.5) * (tris[1, 6:9] - tris[1, 0:3])   # collinear
+    tris[2, 3:9] = tris[2, 0:6] + np.float32(1e-6)                # tiny
+    dyn = np.concatenate([dyn, tris[5:6, 0:3]], 0).astype(np.float32)   # on a vertex
+    params = scenes.water_params(0.25, h, mass=1.0)
+    return scenes.Scene(name=f"triangle_soup_{seed}", dyn_pos=dyn, static_pos=np.zeros((0, 3), np.float32),
+                        params=params, dt=1e-3, steps=0, triangles=tris)

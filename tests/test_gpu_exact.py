@@ -22,7 +22,7 @@ import os
 import numpy as np
 import pytest
 
-from oracle_lib import Oracle, coincident_scene, differing_words, random_scene
+from oracle_lib import Oracle, coincident_scene, differing_words, random_scene, triangle_soup_scene
 from sphfluidsimulation_gb300 import scenes
 from sphfluidsimulation_gb300.engine import SimulationEngineCUDA
 
@@ -287,3 +287,20 @@ def test_exact_random_scenes(seed):
         e.update(sc.dt, steps)
         diff = differing_words(e.read_dynamic_buffer(), o.read_raw())
         assert not diff.any(), f"{sc.name}: {int(diff.any(1).sum())} particles differ, per field {diff.sum(0)}"
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_exact_triangle_soup(seed):
+    """Degenerate triangles (two equal vertices, collinear, tiny) and a
+    particle exactly on a vertex, where CalculateTriangleForce divides by a
+    zero distance and the particle turns NaN: three exact steps equal the
+    oracle word for word (NaN where it has NaN)."""
+    sc = triangle_soup_scene(seed)
+    o = Oracle(0)
+    o.init(sc)
+    e = exact_engine(sc)
+    for step in range(1, 4):
+        o.update(sc.dt, 1)
+        e.update(sc.dt, 1)
+        diff = differing_words(e.read_dynamic_buffer(), o.read_raw())
+        assert not diff.any(), f"after {step} steps: {int(diff.any(1).sum())} particles differ, per field {diff.sum(0)}"

@@ -7,7 +7,8 @@ import os
 import numpy as np
 import pytest
 
-from oracle_lib import REF_SO, Oracle, RefEngine, coincident_scene, differing_words, oracle_counting_sort, oracle_hash
+from oracle_lib import (REF_SO, Oracle, RefEngine, coincident_scene, differing_words, oracle_counting_sort,
+                        oracle_hash, triangle_soup_scene)
 from sphfluidsimulation_gb300 import scenes
 
 GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
@@ -205,6 +206,22 @@ def test_oracle_matches_reference_far_cells():
     r.update(sc.dt, 2)
     assert o.read_raw().tobytes() == r.read_raw().tobytes()
     assert all(np.array_equal(x, y) for x, y in zip(o.maps(), r.maps()))
+
+
+@pytest.mark.skipif(not os.path.exists(REF_SO), reason="reference not compiled here (no reference tree)")
+def test_oracle_matches_reference_triangle_soup():
+    """Degenerate triangles and a particle on a vertex (tests/oracle_lib
+    triangle_soup_scene): the oracle's CalculateTriangleForce gives the
+    reference's bytes, NaN included."""
+    for seed in (1, 2):
+        sc = triangle_soup_scene(seed)
+        o, r = Oracle(0), RefEngine()
+        o.init(sc)
+        r.init(sc)
+        for steps in (1, 2):
+            o.update(sc.dt, steps)
+            r.update(sc.dt, steps)
+            assert not differing_words(o.read_raw(), r.read_raw()).any(), (seed, steps)
 
 
 def test_reorder_cadence_and_identity():
