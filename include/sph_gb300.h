@@ -132,8 +132,9 @@ SPH_API sph_status sph_engine_read_dynamic(sph_engine* engine, sph_dynamic_parti
  * reordering step, SF:332-345), i.e. the bytes LockRead() returns there. */
 SPH_API sph_status sph_engine_read_dynamic_buffer(sph_engine* engine, sph_dynamic_particle* out);
 
-/* LockWrite()-style upload: replaces every particle's position and velocity
- * (input order; pressure and hash are ignored) and re-sorts. */
+/* LockWrite()-style upload: replaces every particle's position, pressure and
+ * velocity (input order; the hash is recomputed from the position) and
+ * re-sorts.  The pressure stays until the next step's density pass. */
 SPH_API sph_status sph_engine_write_dynamic(sph_engine* engine, const sph_dynamic_particle* in);
 
 /* The same upload left queued on the engine's stream, like the OpenCL

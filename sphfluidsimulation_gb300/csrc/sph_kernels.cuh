@@ -430,7 +430,8 @@ __device__ __forceinline__ void gather_tile(const Tile& tile, const SceneDesc* s
                                             const uint32_t* arrival, const uint32_t* ptag, const uint32_t* start,
                                             const float4* pos_src, const float4* vel_src, float4* pos_dst,
                                             float4* vel_dst, uint32_t* tag_dst, uint32_t assign, uint32_t* err,
-                                            const float4* accel_src = nullptr, float4* accel_dst = nullptr)
+                                            const float4* accel_src = nullptr, float4* accel_dst = nullptr,
+                                            const uint32_t* tag_keep = nullptr)
 {
     const SceneDesc& sc = scenes[tile.scene];
     const uint32_t j = tile.begin + threadIdx.x;
@@ -456,7 +457,9 @@ __device__ __forceinline__ void gather_tile(const Tile& tile, const SceneDesc* s
     if (accel_src) accel_dst[dst] = accel_src[j];
     if (assign != kTagNone) {
         const bool renumber = assign == kTagSlot || (assign == kTagStep && sc.reorder);
-        tag_dst[dst] = renumber ? dst - sc.p_off : mine;
+        // tag_keep: the ranking key is not the tag (a write ranks by the slot
+        // each particle had before it); the tag comes from the source slot
+        tag_dst[dst] = renumber ? dst - sc.p_off : (tag_keep ? tag_keep[j] : mine);
     }
 }
 

@@ -28,6 +28,7 @@ struct SortArgs {
     uint32_t assign;            // TagAssign
     const float4* accel_src;    // recorded acceleration per source slot, moved along (or null)
     float4* accel_dst;
+    const uint32_t* tag_keep;   // kTagKeep: tag per source slot when tag_src is only a ranking key
     uint32_t* count;
     uint32_t* start;
     uint32_t* err;
@@ -172,6 +173,7 @@ public:
     uint32_t *key = nullptr, *arrival = nullptr, *ptag = nullptr, *count = nullptr, *start = nullptr;
     uint32_t* tag = nullptr;       // buffer tag per sorted slot
     uint32_t* tag_io = nullptr;    // tags in caller's order while a write re-sorts
+    uint32_t* rank_io = nullptr;   // ~(slot before the write) in caller's order: the write's ranking key
     unsigned long long* scan_status = nullptr;
     uint32_t* scan_ticket = nullptr;
     uint32_t* err = nullptr;

@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(kTileThreads) k_scatter(SortArgs a)
 __global__ void __launch_bounds__(kTileThreads) k_gather(SortArgs a)
 {
     gather_tile(a.tiles[blockIdx.x], a.scenes, a.key, a.arrival, a.ptag, a.start, a.pos_src, a.vel_src,
-                a.pos_dst, a.vel_dst, a.tag_dst, a.assign, a.err, a.accel_src, a.accel_dst);
+                a.pos_dst, a.vel_dst, a.tag_dst, a.assign, a.err, a.accel_src, a.accel_dst, a.tag_keep);
     if (a.nonfinite_rotate && blockIdx.x == 0 && threadIdx.x == 0) {   // the force pass has finished
         a.nonfinite_rotate[0] = a.nonfinite_rotate[1];
         a.nonfinite_rotate[1] = 0u;
@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(kTileThreads) k_static_bitmap(const Tile* tile
 __global__ void __launch_bounds__(kTileThreads) k_unsort(const Tile* tiles, const SceneDesc* scenes, const float4* pos,
                                                          const float4* vel, float4* out, const float4* accel_in,
                                                          float4* accel_out, const uint32_t* tag_in, uint32_t* tag_out,
-                                                         int by_tag)
+                                                         int by_tag, uint32_t* rank_out = nullptr)
 {
     const Tile tile = tiles[blockIdx.x];
     const SceneDesc& sc = scenes[tile.scene];
@@ -229,6 +229,7 @@ __global__ void __launch_bounds__(kTileThreads) k_unsort(const Tile* tiles, cons
     if (id >= sc.n) return;
     const uint32_t o = sc.p_off + id;
     if (tag_out) tag_out[o] = tag_in[i];
+    if (rank_out) rank_out[o] = ~i;   // larger for earlier slots: ranking by it keeps the order
     if (!out) return;   // tags only
     const float4 v = vel[i];
     const uint32_t key = fast_mod(cell_hash(p.x, p.y, p.z, sc.h), sc.fm_b);
@@ -237,8 +238,10 @@ __global__ void __launch_bounds__(kTileThreads) k_unsort(const Tile* tiles, cons
     if (accel_in) accel_out[o] = accel_in[i];
 }
 
-// Upload staging (caller's order, positions and velocities as float4 pairs)
-// -> unsorted tmp arrays with the input index in pos.w.
+// Upload staging (caller's order, the reference's 32-byte records as float4
+// pairs: position + pressure, velocity + hash) -> unsorted tmp arrays with
+// the input index in pos.w and the record's pressure in vel.w, which a
+// LockWrite-style upload keeps until the next density pass.
 // Dynamic particles carry their input index in w; static particles carry
 // the Morton code of their cell, which the neighbour passes compare against
 // the cell being visited.
@@ -253,7 +256,7 @@ __global__ void __launch_bounds__(kTileThreads) k_load(const Tile* tiles, const 
     const float4 v = in[2 * (size_t)i + 1];
     const uint32_t w = statics ? cell_hash(p.x, p.y, p.z, sc.h) : i - sc.p_off;
     pos_tmp[i] = make_float4(p.x, p.y, p.z, __uint_as_float(w));
-    vel_tmp[i] = make_float4(v.x, v.y, v.z, 0.f);
+    vel_tmp[i] = make_float4(v.x, v.y, v.z, statics ? 0.f : p.w);
 }
 
 // ---------------------------------------------------------------------------
@@ -314,7 +317,7 @@ void StepState::release()
                     ptag, count, start, scan_status, scan_ticket, err, bar, nonfinite, spos, sstart, spos_ref,
                     sstart_ref, tris,
                     accel, accel_tmp, accel_io, staging, d_tmp_tiles_, d_tmp_scene_, nbr, snbr, ncount, tile_overflow,
-                    saved_pos_, saved_vel_, saved_start_, sbitmap, tag, tag_io, saved_tag_, tri_cells, tri_list,
+                    saved_pos_, saved_vel_, saved_start_, sbitmap, tag, tag_io, rank_io, saved_tag_, tri_cells, tri_list,
                     render_zkey_, render_rgba_, render_depth_};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -322,7 +325,7 @@ void StepState::release()
     if (err_host_) { cudaFreeHost(err_host_); err_host_ = nullptr; }
     saved_pos_ = saved_vel_ = nullptr;
     saved_start_ = nullptr;
-    tag = tag_io = saved_tag_ = nullptr;
+    tag = tag_io = rank_io = saved_tag_ = nullptr;
     tri_cells = tri_list = nullptr;
     render_zkey_ = nullptr;
     render_rgba_ = nullptr;
@@ -761,6 +764,7 @@ sph_status StepState::grow_arena(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s,
     if (accel) { cudaFree(accel); accel = nullptr; }
     if (accel_tmp) { cudaFree(accel_tmp); accel_tmp = nullptr; }
     if (accel_io) { cudaFree(accel_io); accel_io = nullptr; }
+    if (rank_io) { cudaFree(rank_io); rank_io = nullptr; }
     max_tiles_ = tiles_for(cap_n) + max_scenes_;
     cap_n_ = cap_n;
     cap_q_ = cap_q;
@@ -908,8 +912,9 @@ sph_status StepState::enqueue_sort(int kind, bool keep_tags)
     const std::vector<Tile>& tl = kind == 0 ? tiles : stiles;
     if (tl.empty()) return SPH_OK;
     SortArgs a = sort_args(kind);
-    if (keep_tags) {   // a write between steps: every particle keeps its tag
-        a.tag_src = tag_io;
+    if (keep_tags) {   // a write between steps: rank by the slot before it, keep the tag
+        a.tag_src = rank_io;
+        a.tag_keep = tag_io;
         a.assign = kTagKeep;
     }
     const uint32_t len = kind == 0 ? scan_len : (kind == 1 ? sscan_len : sfscan_len);
@@ -1220,12 +1225,20 @@ sph_status StepState::write_scene(uint32_t scene, const sph_dynamic_particle* in
     if (scene >= scenes.size()) return SPH_ERR_NOT_FOUND;
     const SceneDesc& d = scenes[scene];
     if (!d.n) return SPH_OK;
-    // move the current sorted state of all scenes, and their buffer tags, into
-    // staging order first (a lone scene is replaced whole: its tags only); the
-    // re-sort keeps every particle's tag
+    // move the current sorted state of all scenes, their buffer tags and their
+    // slots into staging order first (a lone scene is replaced whole: its tags
+    // and slots only).  The re-sort keeps every particle's tag, and inside a
+    // bucket keeps the order the particles had: the reference's LockWrite
+    // changes the buffer, not its maps, so a written-back state must visit its
+    // neighbours as before (after a reordering step that order is by rising
+    // tag, after a map-mode step by falling tag).
+    if (!rank_io) {
+        sph_status st = dev_alloc(&rank_io, cap_n_);
+        if (st != SPH_OK) return st;
+    }
     k_unsort<<<(unsigned)tiles.size(), kTileThreads, 0, stream_>>>(d_tiles, d_scenes, pos, vel,
                                                                    scenes.size() > 1 ? staging : nullptr, nullptr,
-                                                                   nullptr, tag, tag_io, 0);
+                                                                   nullptr, tag, tag_io, 0, rank_io);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaMemcpyAsync(staging + 2ull * d.p_off, in, sizeof(sph_dynamic_particle) * d.n, cudaMemcpyHostToDevice, stream_));
     sph_status st = enqueue_load(staging, false);

@@ -304,3 +304,22 @@ def test_exact_triangle_soup(seed):
         e.update(sc.dt, 1)
         diff = differing_words(e.read_dynamic_buffer(), o.read_raw())
         assert not diff.any(), f"after {step} steps: {int(diff.any(1).sum())} particles differ, per field {diff.sum(0)}"
+
+
+@pytest.mark.parametrize("interval", [float(np.finfo(np.float32).max), -1.0], ids=["map", "reorder_each_call"])
+def test_exact_write_back_keeps_the_reference_state(interval):
+    """Writing the engine's own state back (sph_engine_write_dynamic, caller's
+    order) between Update calls re-sorts with every particle's buffer tag
+    kept, so the run stays the reference's: after 3 + write + 4 + write + 5
+    steps the bytes equal the oracle's 12 uninterrupted steps, in map mode
+    and reordering on every call."""
+    sc = walled_dam()
+    sc.reorder_interval = interval
+    o = Oracle(0)
+    o.init(sc)
+    e = exact_engine(sc)
+    for steps in (3, 4, 5):
+        o.update(sc.dt, steps)
+        e.update(sc.dt, steps)
+        e.write_dynamic(e.read_dynamic())
+    assert_same_bits(e.read_dynamic_buffer(), o.read_raw(), "after writes")
