@@ -323,3 +323,25 @@ def test_exact_write_back_keeps_the_reference_state(interval):
         e.update(sc.dt, steps)
         e.write_dynamic(e.read_dynamic())
     assert_same_bits(e.read_dynamic_buffer(), o.read_raw(), "after writes")
+
+
+def test_exact_after_reinitialising_the_engine():
+    """One engine, two scenes: after a run that turned particles NaN (the
+    coincident scene) the same engine initialised with a walled dam break
+    that reorders on every call gives the oracle's bytes: no state of the
+    first run (step graph, reorder clock, non-finite flag, tags) survives
+    Initialize (SimulationEngineCPU.cpp:396-419 clears first)."""
+    first = coincident_scene()
+    e = exact_engine(first)
+    e.update(first.dt, 3)
+    assert np.isnan(e.read_dynamic_buffer()["pos"]).any()
+    sc = walled_dam()
+    sc.reorder_interval = -1.0
+    e.initialize(sc)
+    e.set_exact(True)
+    o = Oracle(0)
+    o.init(sc)
+    for steps in (2, 3):
+        o.update(sc.dt, steps)
+        e.update(sc.dt, steps)
+    assert_same_bits(e.read_dynamic_buffer(), o.read_raw(), "second scene")
