@@ -345,3 +345,28 @@ def test_exact_after_reinitialising_the_engine():
         o.update(sc.dt, steps)
         e.update(sc.dt, steps)
     assert_same_bits(e.read_dynamic_buffer(), o.read_raw(), "second scene")
+
+
+@pytest.mark.parametrize("interval", [float(np.finfo(np.float32).max), -1.0], ids=["map", "reorder_each_call"])
+def test_exact_recorded_acceleration(interval):
+    """The recorded acceleration F/rho + g of the last step
+    (sph_engine_record_acceleration, SF:638-641) is the oracle's, bit for
+    bit, with walls and in both reorder modes."""
+    sc = walled_dam()
+    sc.reorder_interval = interval
+    o = Oracle(0)
+    o.init(sc)
+    o.record_accel(True)
+    e = exact_engine(sc)
+    e.record_acceleration(True)
+    o.update(sc.dt, 4)
+    e.update(sc.dt, 4)
+    # the oracle records per slot of the step's input buffer, which a
+    # reordering step then permutes: map through the order before the step
+    _, _, io = o.maps()
+    o.update(sc.dt, 1)
+    e.update(sc.dt, 1)
+    ref = np.empty((sc.n, 3), np.float32)
+    ref[io] = o.accel().astype(np.float32)          # the oracle's floats, widened to double on read
+    got = e.read_acceleration()
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
