@@ -417,6 +417,10 @@ def main():
                     help="time step in s (default: the workload's configured 1e-4)")
     ap.add_argument("--exact", action="store_true",
                     help="time the reference's arithmetic (sph_engine_set_exact) instead of the fused form")
+    ap.add_argument("--served-jobs", type=int, default=200,
+                    help="--workload served: jobs taken from the 2,000-job mix")
+    ap.add_argument("--served-horizon-scale", type=float, default=0.1,
+                    help="--workload served: factor on every job's horizon")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the bounded batched/served samples in the default line")

@@ -351,6 +351,12 @@ SPH_API sph_status sph_server_poll(sph_server* server, uint32_t chunk_steps, uin
 /* Neighbour-pass arithmetic of every job, as sph_engine_set_exact. */
 SPH_API sph_status sph_server_set_exact(sph_server* server, int exact);
 
+/* Ids of the jobs retired since the last call, oldest first: up to
+ * `capacity` of them are moved into job_ids and *count says how many (the
+ * rest stay for the next call).  A caller polls, then fetches just these. */
+SPH_API sph_status sph_server_finished(sph_server* server, uint64_t* job_ids, uint32_t capacity,
+                                       uint32_t* count);
+
 /* Retrieves a finished job's particles (input order, n entries) and
  * densities (n floats, rho = p/k + rho0); may be NULL.  Returns
  * SPH_ERR_NOT_FOUND while the job is unfinished. */

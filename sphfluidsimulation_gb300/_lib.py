@@ -104,6 +104,7 @@ _SIGS = {
                                 C.c_uint32, _u64p]),
     "sph_server_poll": (_st, [_vp, C.c_uint32, _up, _up]),
     "sph_server_result": (_st, [_vp, C.c_uint64, _vp, _fp]),
+    "sph_server_finished": (_st, [_vp, C.POINTER(C.c_uint64), C.c_uint32, _up]),
     "sph_server_job_bytes": (C.c_uint64, [C.c_uint32, C.c_uint32]),
 }
 

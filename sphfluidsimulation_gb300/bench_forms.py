@@ -131,7 +131,9 @@ def _served(jobset, arrivals, budget: int, slots: int, chunk: int):
             continue
         t0 = time.perf_counter()
         srv.poll(chunk)
-        done = [jid for jid in in_flight if srv.result(jid) is not None]
+        done = srv.finished()                  # only the retired jobs are fetched
+        for jid in done:
+            srv.result(jid)
         clock += time.perf_counter() - t0
         for jid in done:
             idx = in_flight.pop(jid)
@@ -188,7 +190,8 @@ def run(args, world, rank, local, pg) -> Dict:
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam breaks)",
                 "config": {"workload": "batched_96", "particles": r["particles"]}, "batched": r,
                 "gpu_launches": args.steps}
-    r = run_served(pg=pg, world=world, rank=rank)
+    r = run_served(n_jobs=getattr(args, "served_jobs", 200), horizon_scale=getattr(args, "served_horizon_scale", 0.1),
+                   pg=pg, world=world, rank=rank)
     return {"metric": "aggregate particle-steps/s, served jobs", "value": r["served_particle_steps_per_s"],
             "unit": "particle-steps/s", "n_gpus": world, "steps": None, "warmup": 1,
             "ms_per_step": None, "higher_is_better": True, "scaling": "strong", "vs_baseline": None,

@@ -152,6 +152,7 @@ struct sph_server {
     std::unordered_map<uint64_t, std::unique_ptr<Job>> jobs;
     std::deque<uint64_t> queue;
     std::vector<uint64_t> active;
+    std::deque<uint64_t> finished;   // retired since the last sph_server_finished
     bool dirty = false;
     sph::StepMode mode = sph::StepMode::Staged;
 };
@@ -388,6 +389,7 @@ SPH_API sph_status sph_server_poll(sph_server* sv, uint32_t chunk_steps, uint32_
                 SRV_TRY(sv->arena.read_scene((uint32_t)k, j.result.data(), nullptr));
                 j.state = JobState::Finished;
                 release_ranges(sv, j);
+                sv->finished.push_back(j.id);
                 sv->dirty = true;
             } else {
                 still.push_back(j.id);
@@ -397,6 +399,18 @@ SPH_API sph_status sph_server_poll(sph_server* sv, uint32_t chunk_steps, uint32_
     }
     if (active_out) *active_out = (uint32_t)sv->active.size();
     if (queued_out) *queued_out = (uint32_t)sv->queue.size();
+    return SPH_OK;
+}
+
+SPH_API sph_status sph_server_finished(sph_server* sv, uint64_t* job_ids, uint32_t capacity, uint32_t* count)
+{
+    if (!sv || !count || (capacity && !job_ids)) return SPH_ERR_INVALID_ARGUMENT;
+    uint32_t k = 0;
+    while (k < capacity && !sv->finished.empty()) {
+        job_ids[k++] = sv->finished.front();
+        sv->finished.pop_front();
+    }
+    *count = k;
     return SPH_OK;
 }
 

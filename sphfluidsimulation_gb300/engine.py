@@ -348,6 +348,17 @@ class Server:
         check(self.lib.sph_server_poll(self.h, int(chunk_steps), C.byref(a), C.byref(q)), "sph_server_poll")
         return a.value, q.value
 
+    def finished(self) -> list:
+        """Ids of the jobs retired since the last call (sph_server_finished)."""
+        out = []
+        buf = (C.c_uint64 * 256)()
+        cnt = C.c_uint32()
+        while True:
+            check(self.lib.sph_server_finished(self.h, buf, 256, C.byref(cnt)), "sph_server_finished")
+            out.extend(buf[:cnt.value])
+            if cnt.value < 256:
+                return out
+
     def result(self, job_id: int):
         """(particles, density) of a finished job, or None while it runs."""
         n = self.sizes[job_id]

@@ -151,3 +151,22 @@ def test_served_random_scenes_equal_the_oracle():
         ref = np.empty(sc.n, o.read_raw().dtype)
         ref[io] = o.read_raw()
         assert done[jid][0].tobytes() == ref.tobytes(), sc.name
+
+
+def test_finished_reports_each_job_once():
+    """sph_server_finished drains the ids of retired jobs: every job appears
+    once, in retirement order (the shortest horizon first here), and the
+    results fetched for those ids equal each job run alone."""
+    scs = [job(1200, 9, 21), job(900, 3, 22), job(1500, 14, 23)]
+    srv = Server(budget_bytes=1 << 30, max_slots=2)
+    ids = [srv.submit(sc) for sc in scs]
+    seen = []
+    for _ in range(100):
+        srv.poll(4)
+        seen += srv.finished()
+        if len(seen) == len(ids):
+            break
+    assert sorted(seen) == sorted(ids) and seen[0] == ids[1]
+    assert srv.finished() == []
+    for jid, sc in zip(ids, scs):
+        assert srv.result(jid)[0].tobytes() == alone(sc).tobytes()
