@@ -86,7 +86,9 @@ SPH_API sph_status sph_engine_create(sph_engine** out, int device);
 SPH_API sph_status sph_engine_destroy(sph_engine* engine);
 
 /* SimulationEngine::Clear (SimulationEngineCPU.cpp:365-395): drops the
- * scene, keeps the device arena for reuse. */
+ * scene, keeps the device arrays.  The next sph_engine_initialize reuses
+ * them when the new scene fits (particles, buckets, statics, triangles) and
+ * allocates afresh only when it grows. */
 SPH_API sph_status sph_engine_clear(sph_engine* engine);
 
 /* SimulationEngine::Initialize (SimulationEngineCPU.cpp:396-419) with the

@@ -123,7 +123,7 @@ SPH_API sph_status sph_engine_clear(sph_engine* e)
     if (!e) return SPH_ERR_INVALID_ARGUMENT;
     API_CUDA_TRY(cudaSetDevice(e->device));
     API_CUDA_TRY(cudaStreamSynchronize(e->stream));
-    e->state.release();
+    e->state.drop_scenes();
     e->initialized = false;
     e->sim_time = 0.0;
     e->reorder_elapsed = 0.f;

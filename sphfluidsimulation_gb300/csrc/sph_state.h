@@ -88,7 +88,9 @@ public:
 
     // Lays the scenes out back to back, allocates, uploads and sorts them.
     sph_status build(int device, cudaStream_t stream, const std::vector<SceneInput>& inputs);
-    void release();
+    void release();              // drop_scenes() + free_device_arrays()
+    void drop_scenes();          // forget the scenes, keep the device arrays
+    void free_device_arrays();
 
     // Queues `steps` steps of every scene.  Staged mode replays a captured
     // CUDA graph of the five stage launches; persistent mode issues one
@@ -207,6 +209,7 @@ private:
     sph_status enqueue_scan(uint32_t* cnt, uint32_t* out, uint32_t len, bool cleared = false);
     sph_status alloc_arrays(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s, uint32_t cap_sq, uint32_t cap_sf,
                             uint32_t cap_sbm, uint32_t cap_t, uint32_t max_scenes, uint32_t max_tiles);
+    sph_status zero_state_arrays();
     sph_status enqueue_step_staged(bool record_accel, bool timed);
     sph_status enqueue_step_persistent();
     sph_status ensure_events();

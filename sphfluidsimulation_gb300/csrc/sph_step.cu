@@ -310,9 +310,29 @@ const char* last_error() { return g_last_error.c_str(); }
 
 StepState::~StepState() { release(); }
 
-void StepState::release()
+// Drops the scenes (host tables, the step graph, the triangle cells) and
+// keeps every other device array for the next build.
+void StepState::drop_scenes()
 {
     if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+    if (tri_cells) { cudaFree(tri_cells); tri_cells = nullptr; }
+    if (tri_list) { cudaFree(tri_list); tri_list = nullptr; }
+    scenes.clear();
+    tiles.clear();
+    stiles.clear();
+    tile_first_.clear();
+    total_n = total_s = total_t = 0;
+    scan_len = sscan_len = sfscan_len = 0;
+}
+
+void StepState::release()
+{
+    drop_scenes();
+    free_device_arrays();
+}
+
+void StepState::free_device_arrays()
+{
     void* ptrs[] = {d_scenes, d_sscenes, d_sfscenes, d_tiles, d_stiles, pos, vel, pos_tmp, vel_tmp, key, arrival,
                     ptag, count, start, scan_status, scan_ticket, err, bar, nonfinite, spos, sstart, spos_ref,
                     sstart_ref, tris,
@@ -343,12 +363,6 @@ void StepState::release()
     for (auto& e : events_)
         if (e) cudaEventDestroy(e);
     for (auto& e : events_) e = nullptr;
-    scenes.clear();
-    tiles.clear();
-    stiles.clear();
-    tile_first_.clear();
-    total_n = total_s = total_t = 0;
-    scan_len = sscan_len = sfscan_len = 0;
     cap_n_ = cap_q_ = cap_s_ = cap_sq_ = cap_sf_ = cap_sbm_ = cap_t_ = max_scenes_ = max_tiles_ = 0;
 }
 
@@ -560,13 +574,22 @@ sph_status StepState::alloc_arrays(uint32_t cap_n, uint32_t cap_q, uint32_t cap_
     ALLOC(tris, 9ull * cap_t);
     ALLOC(staging, 2ull * work_n);
 #undef ALLOC
+    return zero_state_arrays();
+}
+
+// Zeroes the arrays the algorithm needs zero at the start of a build: bucket
+// counters, scan status, status words, overflow flags, static bitmaps.
+sph_status StepState::zero_state_arrays()
+{
+    const size_t cnt_len = std::max(std::max(cap_q_, cap_sq_), cap_sf_) + 1ull;
+    const size_t scan_tiles_max = (cnt_len + kScanTile - 1) / kScanTile;
     CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(uint32_t) * cnt_len, stream_));
     CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(uint32_t), stream_));
     CUDA_TRY(cudaMemsetAsync(bar, 0, 2 * sizeof(uint32_t), stream_));
     CUDA_TRY(cudaMemsetAsync(nonfinite, 0, 2 * sizeof(uint32_t), stream_));
     CUDA_TRY(cudaMemsetAsync(scan_status, 0, sizeof(unsigned long long) * scan_tiles_max, stream_));
     CUDA_TRY(cudaMemsetAsync(tile_overflow, 0, sizeof(uint32_t) * max_tiles_, stream_));
-    CUDA_TRY(cudaMemsetAsync(sbitmap, 0, sizeof(uint32_t) * std::max<uint32_t>(cap_sbm, 1), stream_));
+    CUDA_TRY(cudaMemsetAsync(sbitmap, 0, sizeof(uint32_t) * std::max<uint32_t>(cap_sbm_, 1), stream_));
     CUDA_TRY(cudaStreamSynchronize(stream_));
     return SPH_OK;
 }
@@ -595,7 +618,8 @@ static sph_status upload_particles(cudaStream_t stream, float4* staging, uint32_
 
 sph_status StepState::build(int device, cudaStream_t stream, const std::vector<SceneInput>& inputs)
 {
-    release();
+    drop_scenes();
+    if (device != device_ || stream != stream_) free_device_arrays();
     device_ = device;
     stream_ = stream;
     uint64_t p_off = 0, q_off = 0, s_off = 0, sq_off = 0, sf_off = 0, sbm_off = 0, t_off = 0;
@@ -638,9 +662,19 @@ sph_status StepState::build(int device, cudaStream_t stream, const std::vector<S
     scan_len = (uint32_t)q_off + 1u;
     sscan_len = (uint32_t)sq_off + 1u;
     sfscan_len = (uint32_t)sf_off + 1u;
-    sph_status st = alloc_arrays(total_n, (uint32_t)q_off, total_s, (uint32_t)sq_off, (uint32_t)sf_off,
-                                 (uint32_t)sbm_off, total_t, (uint32_t)scenes.size(),
-                                 (uint32_t)std::max(tiles.size(), stiles.size()));
+    // the arrays of an earlier build are reused when every capacity fits
+    const size_t need_tiles = std::max(tiles.size(), stiles.size());
+    const bool fits = pos && total_n <= cap_n_ && q_off <= cap_q_ && total_s <= cap_s_ && sq_off <= cap_sq_ &&
+                      sf_off <= cap_sf_ && sbm_off <= cap_sbm_ && total_t <= cap_t_ &&
+                      scenes.size() <= max_scenes_ && need_tiles <= max_tiles_;
+    sph_status st;
+    if (fits) {
+        st = zero_state_arrays();
+    } else {
+        free_device_arrays();
+        st = alloc_arrays(total_n, (uint32_t)q_off, total_s, (uint32_t)sq_off, (uint32_t)sf_off, (uint32_t)sbm_off,
+                          total_t, (uint32_t)scenes.size(), (uint32_t)need_tiles);
+    }
     if (st != SPH_OK) return st;
     if (!tcells.empty()) {
         if ((st = dev_alloc(&tri_cells, tcells.size())) != SPH_OK) return st;
