@@ -543,9 +543,20 @@ __device__ __forceinline__ uint32_t nb_span(const Neighbourhood& nb)
     return span3(nb.ex0, nb.ex1, nb.ex2) + span3(nb.ey0, nb.ey1, nb.ey2) + span3(nb.ez0, nb.ez1, nb.ez2);
 }
 
+// Distance from its square.  The reference's arithmetic takes the correctly
+// rounded root; the fast form multiplies r^2 by the hardware reciprocal
+// square root (rsqrtf, within 2 ulp), whose value also scales the direction
+// in the force pass.  r^2 = 0 gives 0 and NaN stays NaN in both.
+template <bool kExact>
+__device__ __forceinline__ float root_of(float r2, float rinv)
+{
+    return kExact ? __fsqrt_rn(r2) : (r2 == 0.f ? 0.f : __fmul_rn(r2, rinv));
+}
+
+template <bool kExact>
 __device__ __forceinline__ float w0_of(float r2, float h)
 {
-    const float r = __fsqrt_rn(r2);
+    const float r = root_of<kExact>(r2, kExact ? 0.f : rsqrtf(r2));
     const float w = __fsub_rn(h, r);
     return r >= h ? 0.f : __fmul_rn(__fmul_rn(w, w), w);   // NaN stays NaN (SF:119-125)
 }
@@ -744,21 +755,21 @@ __device__ __forceinline__ void density_tile(uint32_t tile_index, const Tile& ti
                 n0 = ln[0]; n1 = ln[stride]; n2 = ln[2 * (size_t)stride]; n3 = ln[3 * (size_t)stride];
             }
             const float4 q0 = __ldg(pos + j0), q1 = __ldg(pos + j1), q2 = __ldg(pos + j2), q3 = __ldg(pos + j3);
-            sum_d = __fadd_rn(sum_d, w0_of(pair_r2<kExact>(q0, p), h));
-            sum_d = __fadd_rn(sum_d, w0_of(pair_r2<kExact>(q1, p), h));
-            sum_d = __fadd_rn(sum_d, w0_of(pair_r2<kExact>(q2, p), h));
-            sum_d = __fadd_rn(sum_d, w0_of(pair_r2<kExact>(q3, p), h));
+            sum_d = __fadd_rn(sum_d, w0_of<kExact>(pair_r2<kExact>(q0, p), h));
+            sum_d = __fadd_rn(sum_d, w0_of<kExact>(pair_r2<kExact>(q1, p), h));
+            sum_d = __fadd_rn(sum_d, w0_of<kExact>(pair_r2<kExact>(q2, p), h));
+            sum_d = __fadd_rn(sum_d, w0_of<kExact>(pair_r2<kExact>(q3, p), h));
         }
-        for (; m < cnt; ++m, lp += stride) sum_d = __fadd_rn(sum_d, w0_of(pair_r2<kExact>(__ldg(pos + *lp), p), h));
+        for (; m < cnt; ++m, lp += stride) sum_d = __fadd_rn(sum_d, w0_of<kExact>(pair_r2<kExact>(__ldg(pos + *lp), p), h));
         lp = nl.snbr + i;
         for (uint32_t k = 0; k < scnt; ++k, lp += stride)
-            sum_s = __fadd_rn(sum_s, w0_of(pair_r2<kExact>(static_entry_pos(*lp, st), p), h));
+            sum_s = __fadd_rn(sum_s, w0_of<kExact>(pair_r2<kExact>(static_entry_pos(*lp, st), p), h));
     } else {
         // overflow: walk the cells again, summing directly
         walk_neighbours<kExact>(
             sc, i, p, w, pos, start, st,
-            [&](uint32_t, const float4&, float r2) { sum_d = __fadd_rn(sum_d, w0_of(r2, h)); },
-            [&](uint32_t, const float4&, float r2) { sum_s = __fadd_rn(sum_s, w0_of(r2, h)); });
+            [&](uint32_t, const float4&, float r2) { sum_d = __fadd_rn(sum_d, w0_of<kExact>(r2, h)); },
+            [&](uint32_t, const float4&, float r2) { sum_s = __fadd_rn(sum_s, w0_of<kExact>(r2, h)); });
         atomicOr(nl.tile_overflow + tile_index, 1u);   // cleared by the overflow force pass
     }
     nl.ncount[i] = overflow ? (kOverflow | (kOverflow << 16)) : (cnt | (scnt << 16));
@@ -823,7 +834,8 @@ __device__ __forceinline__ void add_dynamic_pair(PairSums& s, const float4& p, c
     float dx = __fsub_rn(q.x, p.x), dy = __fsub_rn(q.y, p.y), dz = __fsub_rn(q.z, p.z);
     const float r2 = kExact ? __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz))
                             : __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-    const float r = __fsqrt_rn(r2);
+    const float rinv = kExact ? 0.f : rsqrtf(r2);
+    const float r = root_of<kExact>(r2, rinv);
     if (r >= h) return;          // a NaN distance is kept (SF:126-139)
     if (r2 == 0.f || r == 0.f) {
         const float3 d = coincident_direction<kExact>(p, tag, i);
@@ -831,8 +843,7 @@ __device__ __forceinline__ void add_dynamic_pair(PairSums& s, const float4& p, c
     } else if (kExact) {
         dx = __fdiv_rn(dx, r); dy = __fdiv_rn(dy, r); dz = __fdiv_rn(dz, r);
     } else {
-        const float inv = __frcp_rn(r);
-        dx = __fmul_rn(dx, inv); dy = __fmul_rn(dy, inv); dz = __fmul_rn(dz, inv);
+        dx = __fmul_rn(dx, rinv); dy = __fmul_rn(dy, rinv); dz = __fmul_rn(dz, rinv);
     }
     const float w = __fsub_rn(h, r);
     const float w1 = __fmul_rn(__fmul_rn(-3.f, w), w);
@@ -866,7 +877,8 @@ __device__ __forceinline__ void add_static_pair(PairSums& s, const float4& p, fl
     float dx = __fsub_rn(q.x, p.x), dy = __fsub_rn(q.y, p.y), dz = __fsub_rn(q.z, p.z);
     const float r2 = kExact ? __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz))
                             : __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-    const float r = __fsqrt_rn(r2);
+    const float rinv = kExact ? 0.f : rsqrtf(r2);
+    const float r = root_of<kExact>(r2, rinv);
     if (r >= h) return;          // a NaN distance is kept (SF:126-139)
     if (r2 == 0.f || r == 0.f) {
         const float3 d = coincident_direction<kExact>(p, tag, i);
@@ -874,8 +886,7 @@ __device__ __forceinline__ void add_static_pair(PairSums& s, const float4& p, fl
     } else if (kExact) {
         dx = __fdiv_rn(dx, r); dy = __fdiv_rn(dy, r); dz = __fdiv_rn(dz, r);
     } else {
-        const float inv = __frcp_rn(r);
-        dx = __fmul_rn(dx, inv); dy = __fmul_rn(dy, inv); dz = __fmul_rn(dz, inv);
+        dx = __fmul_rn(dx, rinv); dy = __fmul_rn(dy, rinv); dz = __fmul_rn(dz, rinv);
     }
     const float w = __fsub_rn(h, r);
     const float w1 = __fmul_rn(__fmul_rn(-3.f, w), w);
