@@ -418,9 +418,9 @@ def main():
     ap.add_argument("--exact", action="store_true",
                     help="time the reference's arithmetic (sph_engine_set_exact) instead of the fused form")
     ap.add_argument("--served-jobs", type=int, default=200,
-                    help="--workload served: jobs taken from the 2,000-job mix")
+                    help="served sample (default line and --workload served): jobs taken from the 2,000-job mix")
     ap.add_argument("--served-horizon-scale", type=float, default=0.1,
-                    help="--workload served: factor on every job's horizon")
+                    help="served sample: factor on every job's horizon")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the bounded batched/served samples in the default line")
@@ -447,11 +447,12 @@ def main():
         b = bench_forms.run_batched(min(args.steps, 20))
         line["batched"] = {k: b[k] for k in ("scenes", "particles", "steps", "batched_particle_steps_per_s",
                                              "plain_looped_particle_steps_per_s", "speedup", "mode")}
-        sv = bench_forms.run_served(n_jobs=64, horizon_scale=0.05)
+        sv = bench_forms.run_served(n_jobs=args.served_jobs, horizon_scale=args.served_horizon_scale)
         line["served"] = {k: sv[k] for k in ("jobs", "horizon_scale", "served_particle_steps_per_s",
                                              "fifo_plain_particle_steps_per_s", "speedup", "served_latency",
                                              "fifo_latency", "load_vs_fifo_capacity")}
-        line["served"]["sample"] = "64 jobs of the 2,000-job mix, horizons x0.05; full run: --workload served"
+        line["served"]["sample"] = (f"{args.served_jobs} jobs of the 2,000-job mix, horizons x{args.served_horizon_scale:g}; "
+                                    "all 2,000: --workload served --served-jobs 2000")
     if rank == 0:
         if scene is not None and not args.no_cpu_baseline and world == 1:
             threads = os.cpu_count() or 1
