@@ -417,7 +417,7 @@ def main():
                     help="time step in s (default: the workload's configured 1e-4)")
     ap.add_argument("--exact", action="store_true",
                     help="time the reference's arithmetic (sph_engine_set_exact) instead of the fused form")
-    ap.add_argument("--served-jobs", type=int, default=200,
+    ap.add_argument("--served-jobs", type=int, default=2000,
                     help="served sample (default line and --workload served): jobs taken from the 2,000-job mix")
     ap.add_argument("--served-horizon-scale", type=float, default=0.1,
                     help="served sample: factor on every job's horizon")
@@ -451,8 +451,8 @@ def main():
         line["served"] = {k: sv[k] for k in ("jobs", "horizon_scale", "served_particle_steps_per_s",
                                              "fifo_plain_particle_steps_per_s", "speedup", "served_latency",
                                              "fifo_latency", "load_vs_fifo_capacity")}
-        line["served"]["sample"] = (f"{args.served_jobs} jobs of the 2,000-job mix, horizons x{args.served_horizon_scale:g}; "
-                                    "all 2,000: --workload served --served-jobs 2000")
+        line["served"]["sample"] = (f"{args.served_jobs} jobs of the 2,000-job mix (Poisson stream), horizons "
+                                    f"x{args.served_horizon_scale:g}; --served-jobs / --served-horizon-scale change it")
     if rank == 0:
         if scene is not None and not args.no_cpu_baseline and world == 1:
             threads = os.cpu_count() or 1

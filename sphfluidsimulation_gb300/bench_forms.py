@@ -190,7 +190,7 @@ def run(args, world, rank, local, pg) -> Dict:
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam breaks)",
                 "config": {"workload": "batched_96", "particles": r["particles"]}, "batched": r,
                 "gpu_launches": args.steps}
-    r = run_served(n_jobs=getattr(args, "served_jobs", 200), horizon_scale=getattr(args, "served_horizon_scale", 0.1),
+    r = run_served(n_jobs=getattr(args, "served_jobs", 2000), horizon_scale=getattr(args, "served_horizon_scale", 0.1),
                    pg=pg, world=world, rank=rank)
     return {"metric": "aggregate particle-steps/s, served jobs", "value": r["served_particle_steps_per_s"],
             "unit": "particle-steps/s", "n_gpus": world, "steps": None, "warmup": 1,
