@@ -7,8 +7,9 @@
 // fit may pass it).  An admitted job is uploaded into its own ranges of one
 // device arena and sorted alone, so admissions and retirements never move
 // another job's state.  Every poll advances all admitted jobs together with
-// persistent step launches (one per step) over the current scene table, by
-// the smallest number of steps any of them still needs (at most chunk_steps),
+// the staged step (its CUDA graph of stage kernels, rebuilt when the scene
+// table changes) over the current scene table, by the smallest number of
+// steps any of them still needs (at most chunk_steps),
 // so each job stops exactly at its horizon; finished jobs are read back and
 // their ranges freed.
 #include <algorithm>
