@@ -649,7 +649,7 @@ __device__ __forceinline__ void walk_neighbours_cells(const SceneDesc& sc, uint3
     for (int a = 0; a < 3; ++a)
 #pragma unroll 1
         for (int b = 0; b < 3; ++b)
-#pragma unroll 1
+#pragma unroll
             for (int c = 0; c < 3; ++c) {
                 const float bd2 = pick3f(a, w.box.x0, 0.f, w.box.x2) + pick3f(b, w.box.y0, 0.f, w.box.y2) +
                                   pick3f(c, w.box.z0, 0.f, w.box.z2);
