@@ -491,6 +491,36 @@ __device__ __forceinline__ float dist2(const float4& q, const float4& p)
 // neighbour and are skipped, provided the 27 bucket ids are distinct (their
 // Morton codes span less than the bucket count); otherwise all 27 are walked.
 
+// L2 residency hints for the neighbour lists (PTX createpolicy and
+// .L2::cache_hint).  The density pass writes the lists and the force pass of
+// the same step reads each entry once: the stores ask L2 to keep the lines
+// (evict_last), the force pass's loads let them go (evict_first).
+__device__ __forceinline__ uint64_t l2_policy_keep()
+{
+    uint64_t pol;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+__device__ __forceinline__ uint64_t l2_policy_drop()
+{
+    uint64_t pol;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+__device__ __forceinline__ void store_list(uint32_t* a, uint32_t v, uint64_t pol)
+{
+    asm volatile("st.global.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(a), "r"(v), "l"(pol) : "memory");
+}
+
+__device__ __forceinline__ uint32_t load_list(const uint32_t* a, uint64_t pol)
+{
+    uint32_t v;
+    asm volatile("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+    return v;
+}
+
 constexpr uint32_t kMaxNbr = 96;        // dynamic neighbours listed per particle
 constexpr uint32_t kMaxSNbr = 48;       // static neighbours listed per particle
 constexpr uint32_t kOverflow = 0xFFFFu;
@@ -727,14 +757,15 @@ __device__ __forceinline__ void density_tile(uint32_t tile_index, const Tile& ti
     const Walk w = make_walk<kExact>(sc, p, st.sbitmap, *nl.nonfinite != 0u);
     const uint32_t stride = nl.stride;
     uint32_t cnt = 0, scnt = 0;
+    const uint64_t keep = l2_policy_keep();
     walk_neighbours<kExact>(
         sc, i, p, w, pos, start, st,
         [&](uint32_t j, const float4&, float) {
-            if (cnt < kMaxNbr) nl.nbr[(size_t)cnt * stride + i] = j;
+            if (cnt < kMaxNbr) store_list(nl.nbr + (size_t)cnt * stride + i, j, keep);
             ++cnt;
         },
         [&](uint32_t e, const float4&, float) {
-            if (scnt < kMaxSNbr) nl.snbr[(size_t)scnt * stride + i] = e;
+            if (scnt < kMaxSNbr) store_list(nl.snbr + (size_t)scnt * stride + i, e, keep);
             ++scnt;
         });
     float sum_d = 0.f, sum_s = 0.f;
@@ -1019,18 +1050,19 @@ __device__ __forceinline__ void force_tile(const Tile& tile, const SceneDesc* sc
             // flight.  The list entries of round r + 1 are loaded while round
             // r's neighbours arrive, so a round waits on one load, not two.
             const uint32_t* lp = nl.nbr + i;
+            const uint64_t drop = l2_policy_drop();
             uint32_t k = 0;
             uint32_t n0 = 0, n1 = 0, n2 = 0, n3 = 0;
             if (SPH_NBR_BATCH == 4 && k + 4 <= cd) {
-                n0 = __ldg(lp); n1 = __ldg(lp + stride); n2 = __ldg(lp + 2 * (size_t)stride);
-                n3 = __ldg(lp + 3 * (size_t)stride);
+                n0 = load_list(lp, drop); n1 = load_list(lp + stride, drop);
+                n2 = load_list(lp + 2 * (size_t)stride, drop); n3 = load_list(lp + 3 * (size_t)stride, drop);
             }
             for (; SPH_NBR_BATCH == 4 && k + 4 <= cd; k += 4, lp += 4 * (size_t)stride) {
                 const uint32_t j0 = n0, j1 = n1, j2 = n2, j3 = n3;
                 if (k + 8 <= cd) {
                     const uint32_t* ln = lp + 4 * (size_t)stride;
-                    n0 = __ldg(ln); n1 = __ldg(ln + stride); n2 = __ldg(ln + 2 * (size_t)stride);
-                    n3 = __ldg(ln + 3 * (size_t)stride);
+                    n0 = load_list(ln, drop); n1 = load_list(ln + stride, drop);
+                    n2 = load_list(ln + 2 * (size_t)stride, drop); n3 = load_list(ln + 3 * (size_t)stride, drop);
                 }
                 const float4 q0 = __ldg(pos + j0), q1 = __ldg(pos + j1), q2 = __ldg(pos + j2), q3 = __ldg(pos + j3);
                 const float4 u0 = __ldg(vel + j0), u1 = __ldg(vel + j1), u2 = __ldg(vel + j2), u3 = __ldg(vel + j3);
@@ -1040,13 +1072,13 @@ __device__ __forceinline__ void force_tile(const Tile& tile, const SceneDesc* sc
                 add_dynamic_pair<kExact>(s, p, v, pi, h, q3, u3, tag, i);
             }
             for (; k < cd; ++k, lp += stride) {
-                const uint32_t j = __ldg(lp);
+                const uint32_t j = load_list(lp, drop);
                 add_dynamic_pair<kExact>(s, p, v, pi, h, __ldg(pos + j), __ldg(vel + j), tag, i);
             }
             const float api = fabsf(pi);
             lp = nl.snbr + i;
             for (uint32_t k = 0; k < cs; ++k, lp += stride)
-                add_static_pair<kExact>(s, p, api, h, static_entry_pos(__ldg(lp), st), tag, i);
+                add_static_pair<kExact>(s, p, api, h, static_entry_pos(load_list(lp, drop), st), tag, i);
             g = sc.q_off + integrate_particle<kRecordAccel, kExact>(sc, i, p, v, rho, s, tm, o.pos_out, o.vel_out,
                                                                     o.key_out, o.accel, o.nonfinite_next);
         }
