@@ -41,7 +41,7 @@ constexpr int kTileThreads = 128;          // slots per tile = threads per CTA
 #define SPH_NBR_BATCH 4
 #endif
 constexpr int kScanThreads = kTileThreads;  // the scan runs inside the fused kernel too
-constexpr int kScanItems = 16;             // per thread
+constexpr int kScanItems = 8;              // per thread
 constexpr int kScanTile = kScanThreads * kScanItems;
 constexpr uint32_t kSpinLimit = 1u << 21;  // bounded waits: ~1-2 s with backoff
 
