@@ -1,6 +1,6 @@
 // Declarations of the Blaze Engine names that the reference's engine headers
-// (SPHFluidSimulation/include/SPH/Core/*.h) use, so the C++ adapter shown in
-// INTEGRATION.md can be compiled against those headers with
+// (SPHFluidSimulation/include/SPH/Core/*.h) use, so the C++ adapter
+// include/adapter/SimulationEngineCUDA.h can be compiled against those headers with
 // `g++ -fsyntax-only` (tests/test_adapter_compiles.py).  Test
 // infrastructure: declarations only, nothing here is linked or run.  The
 // Blaze Engine itself is an un-vendored dependency of the reference.

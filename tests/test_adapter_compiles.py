@@ -1,5 +1,5 @@
-"""The C++ adapter of INTEGRATION.md (`SimulationEngineCUDA :
-SPH::SimulationEngine`) compiles against the reference's own engine headers
+"""The C++ adapter include/adapter/SimulationEngineCUDA.h (`SimulationEngineCUDA
+: SPH::SimulationEngine`) compiles against the reference's own engine headers
 (SPHFluidSimulation/include/SPH/Core/SimulationEngine.h, SceneBlueprint.h,
 ParticleBufferManager.h, ResourceLockGuard.h, Particles.h) and this
 library's C ABI (include/sph_gb300.h).
@@ -8,29 +8,28 @@ The headers need the Blaze Engine, an un-vendored dependency of the
 reference; tests/adapter_shim declares the names they use, and
 oracle/ref_shim the integer and vector types.  The check is
 `g++ -std=c++20 -fsyntax-only`, so nothing is linked or run.  It needs the
-reference tree and is skipped where that is absent.
+reference tree (SPH_REFERENCE_ROOT, default /root/reference) and is skipped
+where that is absent.
 """
 import os
-import re
 import shutil
 import subprocess
 
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REFERENCE_INCLUDE = "/root/reference/SPHFluidSimulation/include"
+REFERENCE_ROOT = os.environ.get("SPH_REFERENCE_ROOT", "/root/reference")
+REFERENCE_INCLUDE = os.path.join(REFERENCE_ROOT, "SPHFluidSimulation", "include")
+ADAPTER = os.path.join(ROOT, "include", "adapter", "SimulationEngineCUDA.h")
 
 
 def adapter_source() -> str:
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    blocks = re.findall(r"```cpp\n(.*?)```", text, flags=re.S)
-    assert blocks, "INTEGRATION.md has no C++ block"
-    src = blocks[0]
+    src = open(ADAPTER).read()
     assert "class SimulationEngineCUDA : public SimulationEngine" in src
     return src
 
 
-def test_adapter_block_is_present():
+def test_adapter_declares_every_engine_member():
     src = adapter_source()
     for member in ("void Clear()", "void Initialize(", "void Update(", "SystemImplementationName()",
                    "GetDynamicParticlesBufferManager()", "GetStaticParticlesBufferManager()",
@@ -41,14 +40,12 @@ def test_adapter_block_is_present():
 @pytest.mark.skipif(not os.path.isdir(REFERENCE_INCLUDE), reason="reference tree not present")
 @pytest.mark.skipif(shutil.which("g++") is None, reason="g++ not present")
 def test_adapter_compiles_against_reference_headers(tmp_path):
-    header = tmp_path / "SimulationEngineCUDA.h"
-    header.write_text(adapter_source())
     unit = tmp_path / "adapter.cpp"
     unit.write_text('#include "SimulationEngineCUDA.h"\n'
                     "// the class is complete and concrete: every pure virtual is overridden\n"
                     "SPH::SimulationEngine* make_engine() { return new SPH::SimulationEngineCUDA(0); }\n")
     cmd = ["g++", "-std=c++20", "-fsyntax-only", "-Wall", "-Wno-unused-variable",
-           "-I", str(tmp_path),
+           "-I", os.path.dirname(ADAPTER),
            "-I", os.path.join(ROOT, "tests", "adapter_shim"),
            "-I", os.path.join(ROOT, "oracle", "ref_shim"),
            "-I", REFERENCE_INCLUDE,

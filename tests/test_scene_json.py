@@ -156,7 +156,8 @@ def test_malformed_json_is_rejected(tmp_path):
         scene_json.load_scene(str(p))
 
 
-ASSETS = "/root/reference/FluidSimulationProject/assets/simulationScenes"
+ASSETS = os.path.join(os.environ.get("SPH_REFERENCE_ROOT", "/root/reference"),
+                      "FluidSimulationProject", "assets", "simulationScenes")
 
 
 @pytest.mark.skipif(not os.path.isdir(ASSETS), reason="reference tree not present")
