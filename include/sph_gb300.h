@@ -274,9 +274,11 @@ SPH_API sph_status sph_cell_sort(int device, const float* pos, uint32_t n, float
  * process exits), so the call makes no allocation; n is limited to 262144 and
  * buckets to 524288, larger requests fail with SPH_ERR_CAPACITY.  The first
  * call on a device looks up that array's device address (with the device
- * current), so make it before any stream capture.  All calls share the
- * array: calls that overlap on the GPU race and must be serialised by the
- * caller. */
+ * current), so make it before any stream capture; after a cudaDeviceReset
+ * the next call looks it up again, since the array then lives in a new
+ * context.  All calls share the array: calls that overlap on the GPU race
+ * and must be serialised by the caller.  On any status other than SPH_OK
+ * the contents of keys, starts and order are undefined. */
 SPH_API sph_status sph_cell_sort_noalloc(const float* pos, uint32_t n, float h, uint32_t buckets,
                                          uint32_t* keys, uint32_t* starts, uint32_t* order, void* stream);
 

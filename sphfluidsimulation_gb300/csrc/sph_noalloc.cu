@@ -15,6 +15,8 @@
 // the last call's contents, so each call clears the parts that must start at
 // zero; calls that overlap on the GPU (different streams, or different host
 // threads on one device) race on it and must be serialised by the caller.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "sph_state.h"
@@ -122,10 +124,59 @@ __global__ void __launch_bounds__(kTileThreads) k_na_order(NoAllocArgs a)
 }
 
 std::mutex g_symbol_mutex;
-uint32_t* g_symbol_ptr[64] = {};   // device address of the scratch, per device ordinal
 
-// Device address of the scratch array on the current device, looked up once
-// per device with that device current.
+// The scratch array's device address, cached per device ordinal together
+// with the id of the context it was looked up in.  cudaDeviceReset destroys
+// the device's primary context and the module holding the array; the next
+// runtime call creates a new context with a new id, whose array may sit at
+// another address.  Context ids (cuCtxGetId) are never reused within a
+// process, so a changed id means the cached address is stale.
+struct ScratchSlot {
+    unsigned long long ctx_id;
+    uint32_t* ptr;
+};
+ScratchSlot g_symbol_slot[64] = {};
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+// Id of the current context (0 when there is none yet).  The two driver
+// functions are resolved through the runtime, so the library does not link
+// against the driver library directly.
+sph_status current_context_id(unsigned long long* id)
+{
+    if (!g_ctx_get_current || !g_ctx_get_id) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1{}, q2{};
+        const cudaError_t e1 = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+        const cudaError_t e2 = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+        if (e1 != cudaSuccess || e2 != cudaSuccess || !f1 || !f2) {
+            set_last_error("sph_cell_sort_noalloc: the driver's cuCtxGetCurrent / cuCtxGetId are unavailable");
+            return SPH_ERR_CUDA;
+        }
+        g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+        g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f2);
+    }
+    CUcontext ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS) {
+        set_last_error("sph_cell_sort_noalloc: cuCtxGetCurrent failed");
+        return SPH_ERR_CUDA;
+    }
+    *id = 0;
+    if (ctx && g_ctx_get_id(ctx, id) != CUDA_SUCCESS) {
+        set_last_error("sph_cell_sort_noalloc: cuCtxGetId failed");
+        return SPH_ERR_CUDA;
+    }
+    return SPH_OK;
+}
+
+// Device address of the scratch array on the current device.  It is looked
+// up with cudaGetSymbolAddress, with the device current, on the first call
+// on each device and again whenever the device's context has changed since
+// (after a cudaDeviceReset).
 sph_status scratch_address(int device, uint32_t** out)
 {
     if (device < 0 || device >= 64) {
@@ -133,16 +184,24 @@ sph_status scratch_address(int device, uint32_t** out)
         return SPH_ERR_INVALID_ARGUMENT;
     }
     std::lock_guard<std::mutex> lock(g_symbol_mutex);
-    if (!g_symbol_ptr[device]) {
+    unsigned long long ctx_id = 0;
+    sph_status st = current_context_id(&ctx_id);
+    if (st != SPH_OK) return st;
+    ScratchSlot& slot = g_symbol_slot[device];
+    if (!slot.ptr || ctx_id == 0 || slot.ctx_id != ctx_id) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
             set_last_error(std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
             return SPH_ERR_CUDA;
         }
-        g_symbol_ptr[device] = static_cast<uint32_t*>(p);
+        // the look-up made the device's primary context current if none was
+        st = current_context_id(&ctx_id);
+        if (st != SPH_OK) return st;
+        slot.ptr = static_cast<uint32_t*>(p);
+        slot.ctx_id = ctx_id;
     }
-    *out = g_symbol_ptr[device];
+    *out = slot.ptr;
     return SPH_OK;
 }
 
