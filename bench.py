@@ -94,7 +94,7 @@ def pair_rates(samples, stage_ms, first_step: int):
         "static_neighbours_per_particle": mean["static_neighbours"] / n,
         "density_candidate_tests_per_s": mean["candidates"] / dens_s if dens_s > 0 else None,
         "force_pair_evals_per_s": in_range / force_s if force_s > 0 else None,
-        "steps_sampled": f"{first_step}..{first_step + 10 * (len(samples) - 1)} every 10",
+        "steps_sampled": f"{first_step}..{first_step + len(samples) - 1}, every step (the timed window)",
     }
 
 
@@ -182,23 +182,24 @@ def max_over_ranks(pg, value: float, local: int) -> float:
 # CPU baseline (the oracle port of the reference CPU engine, threaded)
 # ---------------------------------------------------------------------------
 
-def cpu_baseline(scene, target_s: float, max_steps: int, threads: int):
-    """The oracle port of the reference CPU engine on `threads` host threads:
-    one timed warm-up step sizes the sample to about `target_s` seconds of
-    CPU work (at most `max_steps` steps), then one update() call over those
-    steps is timed.  Returns (particle-steps/s, seconds, steps)."""
+def cpu_baseline(scene, warmup: int, steps: int, threads: int, max_s: float = 60.0):
+    """The oracle port of the reference CPU engine on `threads` host threads,
+    over the GPU arm's window: `warmup` untimed steps, then one update() call
+    over the next `steps` steps, timed.  If one step costs so much that the
+    window would take more than `max_s` seconds, fewer steps are timed (the
+    sample says so).  Returns (particle-steps/s, seconds, steps timed)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_lib import Oracle
     o = Oracle(threads)
     o.init(scene)
     t0 = time.perf_counter()
-    o.update(scene.dt, 1)
-    per_step = max(time.perf_counter() - t0, 1e-6)
-    steps = max(1, min(max_steps, int(target_s / per_step)))
+    o.update(scene.dt, max(1, warmup))
+    per_step = max((time.perf_counter() - t0) / max(1, warmup), 1e-6)
+    timed = max(1, min(steps, int(max_s / per_step)))
     t0 = time.perf_counter()
-    o.update(scene.dt, steps)
+    o.update(scene.dt, timed)
     dt = time.perf_counter() - t0
-    return scene.n * steps / dt, dt, steps
+    return scene.n * timed / dt, dt, timed
 
 
 def run_reference(args):
@@ -208,11 +209,12 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     scene = workload_scene(args.workload if args.workload not in ("batched", "served") else "dam_break_1m", 1,
                            args.dt)
-    # bounded sample: the steps of this run, capped at about a minute of CPU work
-    warm = 1
-    value, secs, steps = cpu_baseline(scene, 60.0, args.steps, threads)
-    sample = (f"{scene.name}: {scene.n} particles, {steps} timed steps after {warm} warm-up, "
-              f"one update() call ({secs:.1f} s)")
+    # the GPU arm's window: W untimed warm-up steps, then K timed steps in
+    # one update() call (capped at about a minute of CPU work)
+    warm = args.warmup
+    value, secs, steps = cpu_baseline(scene, warm, args.steps, threads)
+    sample = (f"{scene.name}: {scene.n} particles, steps {warm + 1}..{warm + steps} timed after {warm} warm-up "
+              f"steps, one update() call ({secs:.1f} s)")
     line = {
         "impl": "reference", "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
         "n_gpus": world, "steps": steps, "warmup": warm, "ms_per_step": 1000.0 * secs / steps,
@@ -246,8 +248,11 @@ def run_plain(args, world, rank, local, pg):
     stream = torch.cuda.ExternalStream(eng.stream_handle(), device=torch.device("cuda", local))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
-    # warm-up (also builds the step graph)
+    # warm-up (also builds the step graph), then a device checkpoint: every
+    # measurement below replays the same steps W+1..W+K from it, bit for bit
     eng.update(scene.dt, args.warmup)
+    eng.save_state()
+    issue_peak = fp32_issue_peak(local)
 
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -272,21 +277,24 @@ def run_plain(args, world, rank, local, pg):
     total_s = max_over_ranks(pg, total_s, local)
     value = world * n * args.steps / total_s
 
-    # per-stage times over the same number of steps (events around each
-    # stage); the median per stage, so a step disturbed by the shared host
-    # does not skew the breakdown
+    # per-stage times over the same steps (events around each stage), and
+    # the neighbour walk's counts at each of them
+    eng.restore_state()
     eng.set_timing(True)
-    per_step, nstats = [], []
+    per_step = []
     for k in range(args.steps):
-        if k % 10 == 0:                           # the walk's counts over the same states
-            nstats.append(eng.neighbour_stats())
         with torch.cuda.stream(stream):
             flush.zero_()
         eng.update(scene.dt, 1)
         per_step.append(eng.kernel_times().astype(np.float64))
     eng.set_timing(False)
-    stage_ms = np.median(np.asarray(per_step), axis=0)
-    pairs = pair_rates(nstats, stage_ms, args.warmup + args.steps)
+    eng.restore_state()
+    nstats = []
+    for k in range(args.steps):
+        nstats.append(eng.neighbour_stats())
+        eng.update(scene.dt, 1)
+    stage_ms = np.mean(np.asarray(per_step), axis=0)
+    pairs = pair_rates(nstats, stage_ms, args.warmup + 1)
     dom = int(np.argmax(stage_ms))
     dom_name = STAGES[dom]
     peak, peak_kind = measured_peaks()
@@ -324,11 +332,14 @@ def run_plain(args, world, rank, local, pg):
                    "arithmetic": "exact (the reference's operations)" if args.exact else "fast (fused)",
                    "parallelism": "replicas" if world > 1 else "single"},
         "stage_ms": dict(zip(STAGES, [round(float(x), 5) for x in stage_ms])),
+        "stage_ms_window": (f"steps {args.warmup + 1}..{args.warmup + args.steps}, replayed from a device "
+                            "checkpoint: the same steps as value, mean per stage"),
+        "stage_sum_ms": round(float(np.sum(stage_ms)), 5),
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                      "alg_bytes_per_launch": alg_bytes(dom_name, n, s)},
         "pairs": pairs,
-        "issue_roofline": issue_roofline(dom_name, args.workload, float(stage_ms[dom]),
+        "issue_roofline": issue_roofline(dom_name, args.workload, float(stage_ms[dom]), issue_peak,
                                          float(clk.get("sm_mhz") or 0.0) if isinstance(clk, dict) else 0.0),
         "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": 32 * n,
                 "d2h_bytes_per_step": 32 * n, "steps": e2e_steps},
@@ -388,21 +399,38 @@ def profiled_traffic(stage: str, workload: str, column: int = 2):
     return None
 
 
-def issue_roofline(stage: str, workload: str, stage_ms: float, sm_mhz: float):
+def fp32_issue_peak(device: int):
+    """The GPU's FP32 issue rate, measured now by the library's FMA
+    microbenchmark (sph_probe_fp32_issue): warp FMA instructions per second
+    with every SM fully occupied."""
+    import ctypes as C
+    from sphfluidsimulation_gb300 import _lib
+    rate, ms = C.c_double(), C.c_float()
+    _lib.check(_lib.load().sph_probe_fp32_issue(int(device), C.byref(rate), C.byref(ms)), "sph_probe_fp32_issue")
+    return {"warp_instructions_per_s": rate.value, "probe_ms": ms.value}
+
+
+def issue_roofline(stage: str, workload: str, stage_ms: float, probe, sm_mhz: float):
     """The bound the neighbour passes actually meet: warp instructions per
-    launch (ncu, committed) over the live launch time, against the issue
-    peak of 152 SMs x 4 schedulers x one warp instruction per cycle at the
-    SM clock sampled during the timed steps."""
+    launch (ncu smsp__inst_executed.sum, mean over the same steps, committed
+    in profiles/ncu_traffic.txt) over the live launch time, against the
+    FP32 issue rate measured by the FMA probe in this run.  The nominal
+    152 SMs x 4 schedulers x the sampled clock is given beside it."""
     inst = profiled_traffic(stage, workload, 3)
-    if inst is None or not sm_mhz:
+    if inst is None or not probe:
         return None
     import torch
     sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
     achieved = inst / (stage_ms * 1e-3)
-    peak = sms * 4 * sm_mhz * 1e6
-    return {"kernel": stage, "achieved": achieved, "peak": peak, "unit": "warp instructions/s",
-            "frac": achieved / peak, "warp_instructions_per_launch": inst,
-            "peak_basis": f"{sms} SMs x 4 schedulers x {sm_mhz:.0f} MHz"}
+    peak = probe["warp_instructions_per_s"]
+    out = {"kernel": stage, "achieved": achieved, "peak": peak, "unit": "warp instructions/s",
+           "frac": achieved / peak, "warp_instructions_per_launch": inst,
+           "peak_basis": "measured: FP32 FMA microbenchmark (sph_probe_fp32_issue) in this run",
+           "probe_ms": probe["probe_ms"]}
+    if sm_mhz:
+        out["nominal_peak"] = sms * 4 * sm_mhz * 1e6
+        out["nominal_basis"] = f"{sms} SMs x 4 schedulers x {sm_mhz:.0f} MHz (sampled)"
+    return out
 
 
 def main():
@@ -450,15 +478,17 @@ def main():
         sv = bench_forms.run_served(n_jobs=args.served_jobs, horizon_scale=args.served_horizon_scale)
         line["served"] = {k: sv[k] for k in ("jobs", "horizon_scale", "served_particle_steps_per_s",
                                              "fifo_plain_particle_steps_per_s", "speedup", "served_latency",
-                                             "fifo_latency", "load_vs_fifo_capacity")}
+                                             "fifo_latency", "load_vs_fifo_capacity", "served_poll_phases",
+                                             "served_makespan_s", "fifo_makespan_s")}
         line["served"]["sample"] = (f"{args.served_jobs} jobs of the 2,000-job mix (Poisson stream), horizons "
                                     f"x{args.served_horizon_scale:g}; --served-jobs / --served-horizon-scale change it")
     if rank == 0:
         if scene is not None and not args.no_cpu_baseline and world == 1:
             threads = os.cpu_count() or 1
-            v, secs, steps = cpu_baseline(scene, 15.0, 1000, threads)
+            v, secs, steps = cpu_baseline(scene, args.warmup, args.steps, threads)
             line["cpu_baseline"] = {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-                                    "sample": f"{scene.name}: {scene.n} particles, {steps} steps after 1 warm-up "
+                                    "sample": f"{scene.name}: {scene.n} particles, steps {args.warmup + 1}.."
+                                              f"{args.warmup + steps} after {args.warmup} warm-up steps "
                                               f"({secs:.1f} s), oracle port of the reference CPU engine"}
         print(json.dumps(line), flush=True)
     if pg is not None:

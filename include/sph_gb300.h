@@ -205,6 +205,24 @@ typedef struct sph_neighbour_stats {
 } sph_neighbour_stats;
 SPH_API sph_status sph_engine_neighbour_stats(sph_engine* engine, sph_neighbour_stats* out);
 
+/* Device-side checkpoint of the scene (one per engine, kept on the device):
+ * save copies the sorted particles, their buffer tags and the bucket table,
+ * restore puts them back together with the simulation time and the reorder
+ * clock, so the steps that follow repeat the saved run bit for bit.  Used to
+ * time and profile several passes over the same steps.  The reference has
+ * no counterpart (its buffers are the caller's, ParticleBufferManager.h:7-25).
+ * A new scene (sph_engine_initialize / clear) discards the copy. */
+SPH_API sph_status sph_engine_save_state(sph_engine* engine);
+SPH_API sph_status sph_engine_restore_state(sph_engine* engine);
+
+/* Measurement: the GPU's FP32 issue rate, measured by a fused multiply-add
+ * microbenchmark (every SM fully occupied, eight independent FMA chains per
+ * thread, CUDA-event timed, at least 50 ms).  warp_fma_per_s = warp FMA
+ * instructions issued per second over the GPU; ms = the timed launch.  It
+ * is the issue-bound roofline of the neighbour passes.  No counterpart in
+ * the reference, which publishes no performance figures. */
+SPH_API sph_status sph_probe_fp32_issue(int device, double* warp_fma_per_s, float* ms);
+
 /* The engine's CUDA stream (a cudaStream_t), for callers that order their
  * own work or timing events with the engine's launches. */
 SPH_API sph_status sph_engine_get_stream(sph_engine* engine, void** stream);
@@ -369,6 +387,13 @@ SPH_API sph_status sph_server_result(sph_server* server, uint64_t job_id, sph_dy
 
 /* Bytes of device state a job of n dynamic and s static particles holds. */
 SPH_API uint64_t sph_server_job_bytes(uint32_t n, uint32_t s);
+
+/* Where the polls' host time went, for measurement: phase_seconds[6] =
+ * admission (uploads and sort launches), waiting for the admissions' sorts,
+ * rebuilding the scene table and step graph, queueing the steps, waiting for
+ * the steps (their device time), reading finished jobs back; counts[3] =
+ * polls, steps run, scene-table rebuilds.  Either may be NULL. */
+SPH_API sph_status sph_server_stats(sph_server* server, double* phase_seconds, uint64_t* counts);
 
 #ifdef __cplusplus
 }

@@ -86,6 +86,9 @@ _SIGS = {
     "sph_engine_kernel_times": (_st, [_vp, _fp, C.c_int]),
     "sph_engine_neighbour_stats": (_st, [_vp, C.POINTER(SphNeighbourStats)]),
     "sph_engine_get_stream": (_st, [_vp, C.POINTER(_vp)]),
+    "sph_probe_fp32_issue": (_st, [C.c_int, _dp, _fp]),
+    "sph_engine_save_state": (_st, [_vp]),
+    "sph_engine_restore_state": (_st, [_vp]),
     "sph_cell_sort": (_st, [C.c_int, _fp, C.c_uint32, C.c_float, C.c_uint32, _up, _up, _up, _up]),
     "sph_cell_sort_noalloc": (_st, [_vp, C.c_uint32, C.c_float, C.c_uint32, _vp, _vp, _vp, _vp]),
     "sph_batch_create": (_st, [C.POINTER(_vp), C.c_int]),
@@ -106,6 +109,7 @@ _SIGS = {
     "sph_server_result": (_st, [_vp, C.c_uint64, _vp, _fp]),
     "sph_server_finished": (_st, [_vp, C.POINTER(C.c_uint64), C.c_uint32, _up]),
     "sph_server_job_bytes": (C.c_uint64, [C.c_uint32, C.c_uint32]),
+    "sph_server_stats": (_st, [_vp, _dp, _u64p]),
 }
 
 _LIB = None

@@ -113,8 +113,9 @@ def _fifo(jobset, arrivals=None):
     return clock, lat
 
 
-def _served(jobset, arrivals, budget: int, slots: int, chunk: int):
-    """Continuous batching.  Returns (makespan, latencies)."""
+def _served(jobset, arrivals, budget: int, slots: int, chunk: int, phases=None):
+    """Continuous batching.  Returns (makespan, latencies); `phases`, when
+    given, receives the server's poll-phase breakdown (sph_server_stats)."""
     srv = Server(budget_bytes=budget, max_slots=slots)
     clock = 0.0
     lat = [None] * len(jobset)
@@ -139,6 +140,8 @@ def _served(jobset, arrivals, budget: int, slots: int, chunk: int):
             idx = in_flight.pop(jid)
             lat[idx] = clock - arrivals[idx]
             finished += 1
+    if phases is not None:
+        phases.update(srv.stats())
     srv.close()
     return clock, lat
 
@@ -159,7 +162,8 @@ def run_served(n_jobs: int = 200, horizon_scale: float = 0.1, seed: int = 0, bud
     _barrier(pg)
     fifo_span, _ = _fifo(jobset)
     _barrier(pg)
-    srv_span, srv_lat_closed = _served(jobset, zeros, budget, slots, chunk)
+    phases = {}
+    srv_span, srv_lat_closed = _served(jobset, zeros, budget, slots, chunk, phases)
     cap_fifo = work / fifo_span
     # Poisson arrivals at 80 % of the FIFO plain capacity
     mean_work = work / n_jobs
@@ -177,7 +181,9 @@ def run_served(n_jobs: int = 200, horizon_scale: float = 0.1, seed: int = 0, bud
             "served_particle_steps_per_s": served_rate, "fifo_plain_particle_steps_per_s": fifo_rate,
             "speedup": served_rate / fifo_rate, "arrival_rate_per_s": rate, "load_vs_fifo_capacity": 0.8,
             "served_latency": _percentiles(srv_lat), "fifo_latency": _percentiles(fifo_lat),
-            "budget_bytes": budget, "slots": slots, "chunk_steps": chunk}
+            "budget_bytes": budget, "slots": slots, "chunk_steps": chunk,
+            "served_poll_phases": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in phases.items()},
+            "served_makespan_s": srv_span, "fifo_makespan_s": fifo_span}
 
 
 def run(args, world, rank, local, pg) -> Dict:

@@ -28,6 +28,9 @@ struct sph_engine {
     bool timing = false;
     bool accel_valid = false;
     uint32_t n = 0, s = 0, t = 0;
+    bool saved = false;             // sph_engine_save_state holds a copy
+    double saved_time = 0.0;
+    float saved_elapsed = 0.f;
 };
 
 struct sph_batch {
@@ -129,6 +132,7 @@ SPH_API sph_status sph_engine_clear(sph_engine* e)
     e->reorder_elapsed = 0.f;
     e->n = e->s = e->t = 0;
     e->accel_valid = false;
+    e->saved = false;
     return SPH_OK;
 }
 
@@ -338,6 +342,36 @@ SPH_API sph_status sph_engine_neighbour_stats(sph_engine* e, sph_neighbour_stats
     out->warp_slots = v[2];
     out->neighbours = v[3];
     out->static_neighbours = v[4];
+    return SPH_OK;
+}
+
+SPH_API sph_status sph_engine_save_state(sph_engine* e)
+{
+    if (!e) return SPH_ERR_INVALID_ARGUMENT;
+    if (!e->initialized) {
+        sph::set_last_error("sph_engine_save_state: no scene");
+        return SPH_ERR_NOT_INITIALIZED;
+    }
+    API_CUDA_TRY(cudaSetDevice(e->device));
+    if (e->n) API_TRY(e->state.save_state());
+    e->saved = true;
+    e->saved_time = e->sim_time;
+    e->saved_elapsed = e->reorder_elapsed;
+    return SPH_OK;
+}
+
+SPH_API sph_status sph_engine_restore_state(sph_engine* e)
+{
+    if (!e) return SPH_ERR_INVALID_ARGUMENT;
+    if (!e->initialized || !e->saved) {
+        sph::set_last_error("sph_engine_restore_state: nothing saved for this scene");
+        return SPH_ERR_NOT_INITIALIZED;
+    }
+    API_CUDA_TRY(cudaSetDevice(e->device));
+    if (e->n) API_TRY(e->state.restore_state());
+    e->sim_time = e->saved_time;
+    e->reorder_elapsed = e->saved_elapsed;
+    e->accel_valid = false;
     return SPH_OK;
 }
 

@@ -156,6 +156,11 @@ struct sph_server {
     std::deque<uint64_t> finished;   // retired since the last sph_server_finished
     bool dirty = false;
     sph::StepMode mode = sph::StepMode::Staged;
+    // host wall time per poll phase (sph_server_stats): admission (uploads
+    // and sort launches), waiting for the admissions' sorts, rebuilding the
+    // scene table, queueing the steps, waiting for them, reading back
+    double phase_s[6] = {};
+    uint64_t polls = 0, steps_run = 0, table_builds = 0;
 };
 
 #define SRV_CUDA_TRY(expr)                                                                     \
@@ -355,6 +360,13 @@ SPH_API sph_status sph_server_poll(sph_server* sv, uint32_t chunk_steps, uint32_
 {
     if (!sv || chunk_steps == 0) return SPH_ERR_INVALID_ARGUMENT;
     SRV_CUDA_TRY(cudaSetDevice(sv->device));
+    double t = now_s();
+    auto lap = [&](int phase) {
+        const double t1 = now_s();
+        sv->phase_s[phase] += t1 - t;
+        t = t1;
+    };
+    ++sv->polls;
     // admit in arrival order; later jobs may pass one that does not fit
     for (auto it = sv->queue.begin(); it != sv->queue.end() && sv->active.size() < sv->max_slots;) {
         Job& j = *sv->jobs[*it];
@@ -365,22 +377,29 @@ SPH_API sph_status sph_server_poll(sph_server* sv, uint32_t chunk_steps, uint32_
             ++it;
         }
     }
+    lap(0);
     if (!sv->active.empty()) {
         SRV_TRY(sv->arena.check_device_error());   // the admissions' sorts
+        lap(1);
         if (sv->dirty) {
             std::vector<SceneDesc> descs;
             for (uint64_t id : sv->active) descs.push_back(desc_of(*sv->jobs[id]));
             SRV_TRY(sv->arena.set_active(descs));
             sv->dirty = false;
+            ++sv->table_builds;
         }
+        lap(2);
         uint32_t steps = chunk_steps;
         for (uint64_t id : sv->active) {
             const Job& j = *sv->jobs[id];
             steps = std::min(steps, j.steps - j.done);
         }
         SRV_TRY(sv->arena.enqueue_steps(steps, sv->mode, false, false));
+        sv->steps_run += steps;
+        lap(3);
         SRV_CUDA_TRY(cudaStreamSynchronize(sv->stream));
         SRV_TRY(sv->arena.check_device_error());
+        lap(4);
         std::vector<uint64_t> still;
         for (size_t k = 0; k < sv->active.size(); ++k) {
             Job& j = *sv->jobs[sv->active[k]];
@@ -397,9 +416,23 @@ SPH_API sph_status sph_server_poll(sph_server* sv, uint32_t chunk_steps, uint32_
             }
         }
         sv->active.swap(still);
+        lap(5);
     }
     if (active_out) *active_out = (uint32_t)sv->active.size();
     if (queued_out) *queued_out = (uint32_t)sv->queue.size();
+    return SPH_OK;
+}
+
+SPH_API sph_status sph_server_stats(sph_server* sv, double* phase_seconds, uint64_t* counts)
+{
+    if (!sv) return SPH_ERR_INVALID_ARGUMENT;
+    if (phase_seconds)
+        for (int k = 0; k < 6; ++k) phase_seconds[k] = sv->phase_s[k];
+    if (counts) {
+        counts[0] = sv->polls;
+        counts[1] = sv->steps_run;
+        counts[2] = sv->table_builds;
+    }
     return SPH_OK;
 }
 

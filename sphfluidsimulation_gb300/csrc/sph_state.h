@@ -105,7 +105,7 @@ public:
     // Neighbour-pass arithmetic: false fused/fast, true the reference's own.
     void set_exact(bool exact)
     {
-        if (exact != exact_ && graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+        if (exact != exact_) drop_graphs();
         if (exact != exact_) grid_cache_ = 0;
         exact_ = exact;
     }
@@ -221,7 +221,13 @@ private:
 
     int device_ = 0;
     cudaStream_t stream_ = nullptr;
-    cudaGraphExec_t graph_ = nullptr;
+    cudaGraphExec_t graph_ = nullptr;        // one staged step
+    cudaGraphExec_t graph_timed_ = nullptr;  // the same with event records between the stages
+    void drop_graphs()
+    {
+        if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+        if (graph_timed_) { cudaGraphExecDestroy(graph_timed_); graph_timed_ = nullptr; }
+    }
     cudaEvent_t events_[6] = {};
     float stage_ms_[5] = {};
     uint32_t persistent_ctas_ = 0;

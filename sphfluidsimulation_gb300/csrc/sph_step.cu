@@ -314,7 +314,7 @@ StepState::~StepState() { release(); }
 // keeps every other device array for the next build.
 void StepState::drop_scenes()
 {
-    if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+    drop_graphs();
     if (tri_cells) { cudaFree(tri_cells); tri_cells = nullptr; }
     if (tri_list) { cudaFree(tri_list); tri_list = nullptr; }
     scenes.clear();
@@ -762,7 +762,7 @@ sph_status StepState::grow_arena(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s,
     if (cap_n == cap_n_ && cap_q == cap_q_ && cap_s == cap_s_ && cap_sq == cap_sq_ && cap_sf == cap_sf_ &&
         cap_sbm == cap_sbm_)
         return SPH_OK;
-    if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+    drop_graphs();
     const size_t old_work = std::max(cap_n_, cap_s_), new_work = std::max(cap_n, cap_s);
     const size_t old_cnt = std::max(std::max(cap_q_, cap_sq_), cap_sf_) + 1ull;
     const size_t new_cnt = std::max(std::max(cap_q, cap_sq), cap_sf) + 1ull;
@@ -873,7 +873,7 @@ sph_status StepState::set_active(const std::vector<SceneDesc>& descs)
         set_last_error("more scenes than the arena's slots");
         return SPH_ERR_CAPACITY;
     }
-    if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+    drop_graphs();
     scenes = descs;
     tiles.clear();
     tile_first_.clear();
@@ -1040,10 +1040,10 @@ sph_status StepState::launch_step_staged(bool record_accel, bool timed)
         s.accel_src = accel_tmp;
         s.accel_dst = accel;
     }
-    if (timed) CUDA_TRY(cudaEventRecord(events_[0], stream_));
+    if (timed) CUDA_TRY(cudaEventRecordWithFlags(events_[0], stream_, cudaEventRecordExternal));
     k_density<kExact><<<nt, kDensityThreads, 0, stream_>>>(a);
     CUDA_TRY(cudaGetLastError());
-    if (timed) CUDA_TRY(cudaEventRecord(events_[1], stream_));
+    if (timed) CUDA_TRY(cudaEventRecordWithFlags(events_[1], stream_, cudaEventRecordExternal));
     if (record_accel) {
         k_force<true, kExact><<<nt, kTileThreads, 0, stream_>>>(a);
         k_force_overflow<true, kExact><<<overflow_grid(nt), kTileThreads, 0, stream_>>>(a);
@@ -1052,16 +1052,16 @@ sph_status StepState::launch_step_staged(bool record_accel, bool timed)
         k_force_overflow<false, kExact><<<overflow_grid(nt), kTileThreads, 0, stream_>>>(a);
     }
     CUDA_TRY(cudaGetLastError());
-    if (timed) CUDA_TRY(cudaEventRecord(events_[2], stream_));
+    if (timed) CUDA_TRY(cudaEventRecordWithFlags(events_[2], stream_, cudaEventRecordExternal));
     sph_status st = enqueue_scan(count, start, scan_len, /*cleared=*/true);
     if (st != SPH_OK) return st;
-    if (timed) CUDA_TRY(cudaEventRecord(events_[3], stream_));
+    if (timed) CUDA_TRY(cudaEventRecordWithFlags(events_[3], stream_, cudaEventRecordExternal));
     k_scatter<<<nt, kTileThreads, 0, stream_>>>(s);
     CUDA_TRY(cudaGetLastError());
-    if (timed) CUDA_TRY(cudaEventRecord(events_[4], stream_));
+    if (timed) CUDA_TRY(cudaEventRecordWithFlags(events_[4], stream_, cudaEventRecordExternal));
     k_gather<<<nt, kTileThreads, 0, stream_>>>(s);
     CUDA_TRY(cudaGetLastError());
-    if (timed) CUDA_TRY(cudaEventRecord(events_[5], stream_));
+    if (timed) CUDA_TRY(cudaEventRecordWithFlags(events_[5], stream_, cudaEventRecordExternal));
     return SPH_OK;
 }
 
@@ -1126,14 +1126,35 @@ sph_status StepState::enqueue_steps(uint32_t steps, StepMode mode, bool record_a
         if (st != SPH_OK) return st;
         st = dev_alloc(&accel_tmp, total_n);
         if (st != SPH_OK) return st;
-        if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+        drop_graphs();
     }
     if (timed) {
         sph_status st = ensure_events();
         if (st != SPH_OK) return st;
         for (float& t : stage_ms_) t = 0.f;
+        // the staged step is timed as it runs untimed: one graph launch per
+        // step, here with event-record nodes between the stages
+        const bool graphed = mode != StepMode::Persistent && !record_accel;
+        if (graphed && !graph_timed_) {
+            cudaGraph_t g = nullptr;
+            CUDA_TRY(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+            st = enqueue_step_staged(false, true);
+            cudaError_t e = cudaStreamEndCapture(stream_, &g);
+            if (st != SPH_OK) { if (g) cudaGraphDestroy(g); return st; }
+            if (e != cudaSuccess) { set_last_error(std::string("graph capture: ") + cudaGetErrorString(e)); return SPH_ERR_CUDA; }
+            e = cudaGraphInstantiate(&graph_timed_, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                graph_timed_ = nullptr;
+                set_last_error(std::string("graph instantiate: ") + cudaGetErrorString(e));
+                return SPH_ERR_CUDA;
+            }
+        }
         for (uint32_t k = 0; k < steps; ++k) {
-            st = (mode == StepMode::Persistent) ? enqueue_step_persistent() : enqueue_step_staged(record_accel, true);
+            if (graphed)
+                CUDA_TRY(cudaGraphLaunch(graph_timed_, stream_));
+            else
+                st = (mode == StepMode::Persistent) ? enqueue_step_persistent() : enqueue_step_staged(record_accel, true);
             if (st != SPH_OK) return st;
             if (mode != StepMode::Persistent) {
                 CUDA_TRY(cudaEventSynchronize(events_[5]));

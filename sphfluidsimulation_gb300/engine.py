@@ -192,6 +192,14 @@ class SimulationEngineCUDA:
         check(self.lib.sph_engine_read_acceleration(self.h, _fptr(out)), "sph_engine_read_acceleration")
         return out
 
+    def save_state(self) -> None:
+        """Device-side checkpoint (sph_engine_save_state)."""
+        check(self.lib.sph_engine_save_state(self.h), "sph_engine_save_state")
+
+    def restore_state(self) -> None:
+        """Back to the checkpoint, bit for bit (sph_engine_restore_state)."""
+        check(self.lib.sph_engine_restore_state(self.h), "sph_engine_restore_state")
+
     def stream_handle(self) -> int:
         """The engine's cudaStream_t as an integer."""
         st = C.c_void_p()
@@ -347,6 +355,17 @@ class Server:
         q = C.c_uint32()
         check(self.lib.sph_server_poll(self.h, int(chunk_steps), C.byref(a), C.byref(q)), "sph_server_poll")
         return a.value, q.value
+
+    PHASES = ("admit", "admit_wait", "table", "enqueue", "steps_wait", "readback")
+
+    def stats(self) -> dict:
+        """Host seconds per poll phase and counts (sph_server_stats)."""
+        sec = (C.c_double * 6)()
+        cnt = (C.c_uint64 * 3)()
+        check(self.lib.sph_server_stats(self.h, sec, cnt), "sph_server_stats")
+        out = {f"{k}_s": float(v) for k, v in zip(self.PHASES, sec)}
+        out.update({"polls": int(cnt[0]), "steps": int(cnt[1]), "table_builds": int(cnt[2])})
+        return out
 
     def finished(self) -> list:
         """Ids of the jobs retired since the last call (sph_server_finished)."""

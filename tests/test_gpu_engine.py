@@ -437,3 +437,43 @@ def test_configured_runs_complete_through_divergence(which):
     assert np.array_equal(np.sort(ids), np.arange(n, dtype=np.uint32))
     keys = d["hash"][ids]
     assert np.array_equal(keys, np.repeat(np.arange(b, dtype=np.uint32), np.diff(starts.astype(np.int64))))
+
+
+def test_save_and_restore_state_replays_bit_for_bit():
+    """sph_engine_save_state / restore_state: the steps after a restore repeat
+    the saved run, all 32 bytes of every particle, and the simulation time
+    comes back with the state; a new scene discards the copy."""
+    sc = small_scene()
+    e = SimulationEngineCUDA()
+    e.initialize(sc)
+    e.update(sc.dt, 3)
+    e.save_state()
+    t0 = e.get_simulation_time()
+    e.update(sc.dt, 7)
+    first = e.read_dynamic_buffer().copy()
+    t1 = e.get_simulation_time()
+    e.restore_state()
+    assert e.get_simulation_time() == t0
+    e.update(sc.dt, 7)
+    assert e.read_dynamic_buffer().tobytes() == first.tobytes()
+    assert e.get_simulation_time() == t1
+    e.initialize(sc)
+    with pytest.raises(SphError):
+        e.restore_state()
+
+
+def test_fp32_issue_probe():
+    """The FMA microbenchmark behind the bench's issue roofline: a positive
+    rate no higher than one warp instruction per scheduler per clock at the
+    GPU's maximum clock (152 SMs x 4 schedulers on GB300)."""
+    import ctypes as C
+    import torch
+    from sphfluidsimulation_gb300 import _lib
+    rate, ms = C.c_double(), C.c_float()
+    _lib.check(_lib.load().sph_probe_fp32_issue(0, C.byref(rate), C.byref(ms)), "sph_probe_fp32_issue")
+    props = torch.cuda.get_device_properties(0)
+    ceiling = props.multi_processor_count * 4 * 2.2e9
+    print(f"fp32 issue: {rate.value:.4e} warp FMA/s over {ms.value:.1f} ms "
+          f"({rate.value / (props.multi_processor_count * 4):.4e} per scheduler per s)")
+    assert ms.value >= 50.0
+    assert 0.2 * ceiling < rate.value <= ceiling
