@@ -251,6 +251,7 @@ def run_plain(args, world, rank, local, pg):
     # warm-up (also builds the step graph), then a device checkpoint: every
     # measurement below replays the same steps W+1..W+K from it, bit for bit
     eng.update(scene.dt, args.warmup)
+    launch = eng.autotune(3)          # launch shapes of the two passes, timed on this state
     eng.save_state()
     issue_peak = fp32_issue_peak(local)
 
@@ -339,6 +340,7 @@ def run_plain(args, world, rank, local, pg):
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                      "alg_bytes_per_launch": alg_bytes(dom_name, n, s)},
         "pairs": pairs,
+        "launch": launch,
         "issue_roofline": issue_roofline(dom_name, args.workload, float(stage_ms[dom]), issue_peak,
                                          float(clk.get("sm_mhz") or 0.0) if isinstance(clk, dict) else 0.0),
         "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": 32 * n,
@@ -474,7 +476,7 @@ def main():
         from sphfluidsimulation_gb300 import bench_forms
         b = bench_forms.run_batched(min(args.steps, 20))
         line["batched"] = {k: b[k] for k in ("scenes", "particles", "steps", "batched_particle_steps_per_s",
-                                             "plain_looped_particle_steps_per_s", "speedup", "mode")}
+                                             "plain_looped_particle_steps_per_s", "speedup", "mode", "launch")}
         sv = bench_forms.run_served(n_jobs=args.served_jobs, horizon_scale=args.served_horizon_scale)
         line["served"] = {k: sv[k] for k in ("jobs", "horizon_scale", "served_particle_steps_per_s",
                                              "fifo_plain_particle_steps_per_s", "speedup", "served_latency",

@@ -205,6 +205,30 @@ typedef struct sph_neighbour_stats {
 } sph_neighbour_stats;
 SPH_API sph_status sph_engine_neighbour_stats(sph_engine* engine, sph_neighbour_stats* out);
 
+/* A step configuration as the autotuner chose it. */
+typedef struct sph_launch_config {
+    int mode;                  /* 0 persistent fused step, 1 staged step graph */
+    uint32_t persistent_ctas;  /* grid of the persistent step (mode 0), else 0 */
+    int density_threads;       /* density pass: threads per CTA ...            */
+    int density_min_ctas;      /* ... and resident CTAs per SM it is built for */
+    int force_threads;         /* the same for the force pass                  */
+    int force_min_ctas;
+    float ms_per_step;         /* measured by the autotuner (or its cache)     */
+    int from_cache;            /* 1: taken from the autotuner's cache          */
+} sph_launch_config;
+
+/* The launch autotuner of sph_batch_autotune for one engine's staged step
+ * (launch shapes of the density and force passes; the engine does not use
+ * the persistent step).  It replaces any sph_engine_save_state copy, since
+ * the trials run on that copy.  out may be NULL. */
+SPH_API sph_status sph_engine_autotune(sph_engine* engine, uint32_t trial_steps, sph_launch_config* out);
+
+/* Sets the launch shapes of the engine's density and force passes by index
+ * (0 = 128 x 7, the default; 1 = 64 x 14; 2 = 256 x 3; 3 = 128 x 6; 4 =
+ * 128 x 8; threads per CTA x resident CTAs per SM), as the autotuner does.
+ * Results do not depend on the shapes. */
+SPH_API sph_status sph_engine_set_launch_shapes(sph_engine* engine, int density_shape, int force_shape);
+
 /* Device-side checkpoint of the scene (one per engine, kept on the device):
  * save copies the sorted particles, their buffer tags and the bucket table,
  * restore puts them back together with the simulation time and the reorder
@@ -330,14 +354,26 @@ SPH_API sph_status sph_batch_set_mode(sph_batch* batch, int mode);
  * exact = 1 each scene's bytes equal the reference CPU engine's. */
 SPH_API sph_status sph_batch_set_exact(sph_batch* batch, int exact);
 
-/* Autotuner: times trial_steps steps of each configuration -- the staged
- * step graph, and the persistent kernel at 1, 2, ... CTAs per SM up to its
- * occupancy limit -- on a saved copy of the state (restored after each
- * trial, so the simulation does not advance), and keeps the fastest.
+/* The launch autotuner.  It times trial_steps steps of each configuration on
+ * a saved copy of the state (restored after each trial, so the simulation
+ * does not advance) and keeps the fastest: the staged step graph with the
+ * density pass under each launch shape (threads per CTA x register-bound
+ * resident CTAs per SM: 128 x 7, the default, 64 x 14, 256 x 3, 128 x 6,
+ * 128 x 8), then the force pass under each shape with the best density
+ * shape, then the persistent kernel at 1, 2, ... CTAs per SM up to its
+ * occupancy limit.  Every shape computes the same bits.  The choice is
+ * cached per GPU and size class (log2 of the particle and scene counts,
+ * arithmetic) in the process, and in the file named by the environment
+ * variable SPH_AUTOTUNE_CACHE when set; a cached class is not timed again.
  * Reports the chosen mode (0 persistent, 1 staged), the persistent grid
- * size (0 when staged) and its time per step (any output may be NULL). */
+ * size (0 when staged) and its time per step (any output may be NULL).
+ * The reference sizes its OpenCL launches from device queries instead
+ * (SimulationEngineGPUKernels.cpp:260-291). */
 SPH_API sph_status sph_batch_autotune(sph_batch* batch, uint32_t trial_steps, int* mode, uint32_t* grid_ctas,
                                       float* ms_per_step);
+
+/* The batch's current configuration (after sph_batch_autotune: its choice). */
+SPH_API sph_status sph_batch_launch_config(sph_batch* batch, sph_launch_config* out);
 
 /* Reads one scene's particles in its input order. */
 SPH_API sph_status sph_batch_read_scene(sph_batch* batch, uint32_t scene_id, sph_dynamic_particle* out);
@@ -364,9 +400,14 @@ SPH_API sph_status sph_server_submit(sph_server* server, const sph_params* param
                                      const float* static_pos, uint32_t s, float dt,
                                      uint32_t steps, uint64_t* job_id);
 
-/* Runs one scheduling round: admits queued jobs that fit, advances every
- * admitted job by up to `chunk_steps` steps in one batched launch sequence,
- * retires finished jobs.  *active and *queued report the state afterwards. */
+/* Runs one scheduling round, pipelined with the GPU: waits for the steps
+ * the previous round queued and retires the jobs they finished (their
+ * readback is queued), admits queued jobs that fit, and queues the next
+ * steps -- every admitted job advanced by up to `chunk_steps` steps in one
+ * batched launch sequence -- then returns while the GPU runs them.  Keep
+ * polling until *active and *queued are 0: the round that finishes the last
+ * jobs is retired by the poll after it.  *active and *queued report the
+ * state afterwards. */
 SPH_API sph_status sph_server_poll(sph_server* server, uint32_t chunk_steps, uint32_t* active,
                                    uint32_t* queued);
 

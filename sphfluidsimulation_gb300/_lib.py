@@ -38,6 +38,12 @@ class SphRenderLayer(C.Structure):
     _fields_ = [("size", C.c_float), ("color", C.c_float * 4)]
 
 
+class SphLaunchConfig(C.Structure):
+    _fields_ = [("mode", C.c_int), ("persistent_ctas", C.c_uint32), ("density_threads", C.c_int),
+                ("density_min_ctas", C.c_int), ("force_threads", C.c_int), ("force_min_ctas", C.c_int),
+                ("ms_per_step", C.c_float), ("from_cache", C.c_int)]
+
+
 class SphNeighbourStats(C.Structure):
     _fields_ = [("particles", C.c_uint64), ("candidates", C.c_uint64), ("warp_slots", C.c_uint64),
                 ("neighbours", C.c_uint64), ("static_neighbours", C.c_uint64)]
@@ -99,6 +105,9 @@ _SIGS = {
     "sph_batch_step": (_st, [_vp, C.c_uint32]),
     "sph_batch_set_mode": (_st, [_vp, C.c_int]),
     "sph_batch_autotune": (_st, [_vp, C.c_uint32, C.POINTER(C.c_int), _up, _fp]),
+    "sph_batch_launch_config": (_st, [_vp, C.POINTER(SphLaunchConfig)]),
+    "sph_engine_autotune": (_st, [_vp, C.c_uint32, C.POINTER(SphLaunchConfig)]),
+    "sph_engine_set_launch_shapes": (_st, [_vp, C.c_int, C.c_int]),
     "sph_batch_read_scene": (_st, [_vp, C.c_uint32, _vp]),
     "sph_batch_info": (_st, [_vp, _u64p, _up, _up]),
     "sph_server_create": (_st, [C.POINTER(_vp), C.c_int, C.c_uint64, C.c_uint32]),

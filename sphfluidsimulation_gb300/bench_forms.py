@@ -52,6 +52,7 @@ def run_batched(steps: int, count: int = 96, seed: int = 0, mode: int = -1, pg=N
     else:
         b.set_mode(mode)
         chosen = None
+    launch = b.launch_config()
     b.step(2)                                   # warm-up
     _barrier(pg)
     t0 = time.perf_counter()
@@ -83,7 +84,7 @@ def run_batched(steps: int, count: int = 96, seed: int = 0, mode: int = -1, pg=N
             "plain_looped_ms_per_step": 1e3 * tp / steps,
             "persistent_grid": [grid, thr],
             "mode": ("autotuned " if chosen else "") + ("persistent" if (chosen[0] if chosen else mode) == 0 else "staged"),
-            "autotune_ms_per_step": chosen[2] if chosen else None}
+            "autotune_ms_per_step": chosen[2] if chosen else None, "launch": launch}
 
 
 def _job_set(n_jobs: int, horizon_scale: float, seed: int):
@@ -124,13 +125,13 @@ def _served(jobset, arrivals, budget: int, slots: int, chunk: int, phases=None):
     n = len(jobset)
     finished = 0
     while finished < n:
+        t0 = time.perf_counter()                # submission (the job's copy) is timed too
         while k < n and arrivals[k] <= clock:
             in_flight[srv.submit(jobset[k][1], steps=jobset[k][0].steps)] = k
             k += 1
         if not in_flight:
             clock = max(clock, arrivals[k])    # idle until the next arrival
             continue
-        t0 = time.perf_counter()
         srv.poll(chunk)
         done = srv.finished()                  # only the retired jobs are fetched
         for jid in done:

@@ -42,6 +42,8 @@ struct sph_batch {
     bool finalized = false;
     StepMode mode = StepMode::Persistent;
     uint32_t grid = 0;
+    sph::TuneChoice tuned{StepMode::Persistent, 0u, 0, 0, 0.f};
+    bool tuned_from_cache = false;
 };
 
 #define API_CUDA_TRY(expr)                                                                     \
@@ -481,54 +483,78 @@ SPH_API sph_status sph_batch_finalize(sph_batch* b)
     return SPH_OK;
 }
 
-// Autotuner: times `trial_steps` steps of the staged graph and of the
-// persistent kernel at 1..max CTAs per SM, on a saved copy of the state
-// (restored after every trial), and keeps the fastest configuration.
+static void fill_config(const StepState& st, const sph::TuneChoice& c, bool from_cache, uint32_t grid,
+                        sph_launch_config* out)
+{
+    if (!out) return;
+    out->mode = c.mode == StepMode::Persistent ? 0 : 1;
+    out->persistent_ctas = c.mode == StepMode::Persistent ? grid : 0u;
+    out->density_threads = sph::kShapeInfo[st.density_shape()].threads;
+    out->density_min_ctas = sph::kShapeInfo[st.density_shape()].min_ctas;
+    out->force_threads = sph::kShapeInfo[st.force_shape()].threads;
+    out->force_min_ctas = sph::kShapeInfo[st.force_shape()].min_ctas;
+    out->ms_per_step = c.ms;
+    out->from_cache = from_cache ? 1 : 0;
+}
+
+// The launch autotuner over the batch (StepState::autotune, staged shapes
+// and persistent grid sizes); the choice is kept for sph_batch_step.
 SPH_API sph_status sph_batch_autotune(sph_batch* b, uint32_t trial_steps, int* mode_out, uint32_t* grid_out,
                                       float* ms_per_step_out)
 {
     if (!b || trial_steps == 0) return SPH_ERR_INVALID_ARGUMENT;
     if (!b->finalized) API_TRY(sph_batch_finalize(b));
     API_CUDA_TRY(cudaSetDevice(b->device));
-    StepState& st = b->state;
-    uint32_t sms = 0, per_sm = 0;
-    API_TRY(st.persistent_capacity(&sms, &per_sm));
-    API_TRY(st.save_state());
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    API_CUDA_TRY(cudaEventCreate(&e0));
-    API_CUDA_TRY(cudaEventCreate(&e1));
-    struct Trial { StepMode mode; uint32_t ctas; float ms; };
-    std::vector<Trial> trials;
-    trials.push_back({StepMode::Staged, 0, 0.f});
-    for (uint32_t c = 1; c <= per_sm; ++c) trials.push_back({StepMode::Persistent, c * sms, 0.f});
-    sph_status result = SPH_OK;
-    for (auto& t : trials) {
-        st.set_persistent_ctas(t.ctas);
-        // one untimed step (graph capture, first-launch costs), then timed steps
-        if ((result = st.enqueue_steps(1, t.mode, false, false)) != SPH_OK) break;
-        if (cudaEventRecord(e0, b->stream) != cudaSuccess) { result = SPH_ERR_CUDA; break; }
-        if ((result = st.enqueue_steps(trial_steps, t.mode, false, false)) != SPH_OK) break;
-        if (cudaEventRecord(e1, b->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) { result = SPH_ERR_CUDA; break; }
-        cudaEventElapsedTime(&t.ms, e0, e1);
-        t.ms /= (float)trial_steps;
-        if ((result = st.check_device_error()) != SPH_OK) break;
-        if ((result = st.restore_state()) != SPH_OK) break;
+    sph::TuneChoice c{};
+    bool cached = false;
+    API_TRY(b->state.autotune(trial_steps, true, &c, &cached));
+    b->mode = c.mode;
+    b->tuned = c;
+    b->tuned_from_cache = cached;
+    API_TRY(b->state.persistent_grid(&b->grid));
+    if (mode_out) *mode_out = c.mode == StepMode::Persistent ? 0 : 1;
+    if (grid_out) *grid_out = c.mode == StepMode::Persistent ? b->grid : 0;
+    if (ms_per_step_out) *ms_per_step_out = c.ms;
+    return SPH_OK;
+}
+
+SPH_API sph_status sph_batch_launch_config(sph_batch* b, sph_launch_config* out)
+{
+    if (!b || !out) return SPH_ERR_INVALID_ARGUMENT;
+    if (!b->finalized) API_TRY(sph_batch_finalize(b));
+    API_CUDA_TRY(cudaSetDevice(b->device));
+    API_TRY(b->state.persistent_grid(&b->grid));
+    sph::TuneChoice c = b->tuned;
+    c.mode = b->mode;
+    fill_config(b->state, c, b->tuned_from_cache, b->grid, out);
+    return SPH_OK;
+}
+
+SPH_API sph_status sph_engine_set_launch_shapes(sph_engine* e, int density_shape, int force_shape)
+{
+    if (!e || density_shape < 0 || density_shape >= sph::kShapeCount || force_shape < 0 ||
+        force_shape >= sph::kShapeCount)
+        return SPH_ERR_INVALID_ARGUMENT;
+    API_CUDA_TRY(cudaSetDevice(e->device));
+    API_CUDA_TRY(cudaStreamSynchronize(e->stream));
+    e->state.set_shapes(density_shape, force_shape);
+    return SPH_OK;
+}
+
+SPH_API sph_status sph_engine_autotune(sph_engine* e, uint32_t trial_steps, sph_launch_config* out)
+{
+    if (!e || trial_steps == 0) return SPH_ERR_INVALID_ARGUMENT;
+    if (!e->initialized || e->n == 0) {
+        sph::set_last_error("sph_engine_autotune: no scene");
+        return SPH_ERR_NOT_INITIALIZED;
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    if (result != SPH_OK) {
-        st.restore_state();
-        return result;
-    }
-    const Trial* best = &trials[0];
-    for (const auto& t : trials)
-        if (t.ms < best->ms) best = &t;
-    b->mode = best->mode;
-    st.set_persistent_ctas(best->ctas);
-    API_TRY(st.persistent_grid(&b->grid));
-    if (mode_out) *mode_out = best->mode == StepMode::Persistent ? 0 : 1;
-    if (grid_out) *grid_out = best->mode == StepMode::Persistent ? best->ctas : 0;
-    if (ms_per_step_out) *ms_per_step_out = best->ms;
+    API_CUDA_TRY(cudaSetDevice(e->device));
+    sph::TuneChoice c{};
+    bool cached = false;
+    e->saved = false;                   // the trials use the engine's checkpoint slot
+    // the trials run with this scene's reorder flag and dt as they stand
+    API_TRY(e->state.autotune(trial_steps, false, &c, &cached));
+    fill_config(e->state, c, cached, 0u, out);
     return SPH_OK;
 }
 

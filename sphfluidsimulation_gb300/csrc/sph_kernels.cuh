@@ -1022,14 +1022,16 @@ struct ForceOut {
     uint32_t* nonfinite_next;   // set when a new position is not finite
 };
 
+// `lane` = the slot's place in the tile (threadIdx.x when a CTA covers one
+// tile; CTAs of other sizes pass theirs).
 template <bool kRecordAccel, bool kExact>
 __device__ __forceinline__ void force_tile(const Tile& tile, const SceneDesc* scenes, const float4* __restrict__ pos,
                                            const float4* __restrict__ vel, const uint32_t* __restrict__ tag,
                                            const StaticTables& st, const TriangleMesh& tm, const NbrArgs& nl,
-                                           const ForceOut& o)
+                                           const ForceOut& o, uint32_t lane = threadIdx.x)
 {
     const SceneDesc& sc = scenes[tile.scene];
-    const uint32_t i = tile.begin + threadIdx.x;
+    const uint32_t i = tile.begin + lane;
     bool valid = i < tile.end;
     uint32_t g = 0;
     if (valid) {
@@ -1122,6 +1124,28 @@ __device__ __forceinline__ void force_overflow_tile(const Tile& tile, const Scen
     }
     const uint32_t r = warp_aggregated_increment(o.count, g, valid);
     if (valid) o.arrival[i] = r;
+}
+
+// ---- views of the step arguments ------------------------------------------
+
+__device__ __forceinline__ NbrArgs nbr_args(const StepArgs& a)
+{
+    return NbrArgs{a.nbr, a.snbr, a.ncount, a.tile_overflow, a.nbr_stride, a.nonfinite};
+}
+
+__device__ __forceinline__ StaticTables static_tables(const StepArgs& a)
+{
+    return StaticTables{a.spos, a.sstart, a.spos_ref, a.sstart_ref, a.sbitmap};
+}
+
+__device__ __forceinline__ TriangleMesh triangle_mesh(const StepArgs& a)
+{
+    return TriangleMesh{a.tris, a.tri_cells, a.tri_list};
+}
+
+__device__ __forceinline__ ForceOut force_out(const StepArgs& a)
+{
+    return ForceOut{a.pos_tmp, a.vel_tmp, a.key, a.arrival, a.count, a.accel, a.nonfinite + 1};
 }
 
 }  // namespace sph

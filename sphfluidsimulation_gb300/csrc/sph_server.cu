@@ -11,7 +11,12 @@
 // table changes) over the current scene table, by the smallest number of
 // steps any of them still needs (at most chunk_steps),
 // so each job stops exactly at its horizon; finished jobs are read back and
-// their ranges freed.
+// their ranges freed.  Polls are pipelined with the GPU: a poll queues its
+// steps and returns, and the next one waits for them, retires the jobs they
+// finished and queues the next round.  On GB300 the kernels read a job's
+// particles from the caller's host arrays and write its results into host
+// memory directly (Grace's address translation), so no host copy or wait
+// sits between rounds.
 #include <algorithm>
 #include <chrono>
 #include <deque>
@@ -118,6 +123,7 @@ struct Job {
     uint64_t p_off = 0, q_off = 0, s_off = 0, sq_off = 0, sf_off = 0, sb_off = 0;
     uint64_t bytes = 0;
     std::vector<sph_dynamic_particle> result;
+    cudaEvent_t ready = nullptr;     // the readback into `result` is complete when this fires
     float gas = 1.f, rho0 = 0.f;
 };
 
@@ -161,6 +167,14 @@ struct sph_server {
     // scene table, queueing the steps, waiting for them, reading back
     double phase_s[6] = {};
     uint64_t polls = 0, steps_run = 0, table_builds = 0;
+    // the GPU reads job inputs and writes results in pageable host memory
+    // itself (GB300: Grace's address translation), so admissions and
+    // readbacks are queued without host copies or waits
+    bool host_direct = false;
+    // steps queued by the last poll, not yet waited for
+    bool pending = false;
+    uint32_t pending_steps = 0;
+    cudaEvent_t steps_done = nullptr;
 };
 
 #define SRV_CUDA_TRY(expr)                                                                     \
@@ -246,11 +260,13 @@ static sph_status admit(sph_server* sv, Job& j)
     SceneInput in = j.in;
     in.pos = j.pos.data();
     in.spos = j.spos.empty() ? nullptr : j.spos.data();
-    SRV_TRY(sv->arena.admit_scene(desc_of(j), in, /*sync=*/false));
-    j.pos.clear();
-    j.pos.shrink_to_fit();
-    j.spos.clear();
-    j.spos.shrink_to_fit();
+    SRV_TRY(sv->arena.admit_scene(desc_of(j), in, /*sync=*/false, sv->host_direct));
+    if (!sv->host_direct) {    // the inputs were copied; kernels read them in place otherwise
+        j.pos.clear();
+        j.pos.shrink_to_fit();
+        j.spos.clear();
+        j.spos.shrink_to_fit();
+    }
     j.state = JobState::Active;
     sv->used_bytes += j.bytes;
     sv->active.push_back(j.id);
@@ -295,6 +311,16 @@ SPH_API sph_status sph_server_create(sph_server** out, int device, uint64_t hbm_
     sv->device = device;
     sv->budget = hbm_budget_bytes;
     sv->max_slots = max_slots;
+    int pageable = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) == cudaSuccess)
+        sv->host_direct = pageable != 0;
+    e = cudaEventCreateWithFlags(&sv->steps_done, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(sv->stream);
+        delete sv;
+        sph::set_last_error(cudaGetErrorString(e));
+        return SPH_ERR_CUDA;
+    }
     *out = sv;
     return SPH_OK;
 }
@@ -304,7 +330,10 @@ SPH_API sph_status sph_server_destroy(sph_server* sv)
     if (!sv) return SPH_ERR_INVALID_ARGUMENT;
     cudaSetDevice(sv->device);
     cudaStreamSynchronize(sv->stream);
+    for (auto& kv : sv->jobs)
+        if (kv.second->ready) cudaEventDestroy(kv.second->ready);
     sv->arena.release();
+    cudaEventDestroy(sv->steps_done);
     cudaStreamDestroy(sv->stream);
     delete sv;
     return SPH_OK;
@@ -356,6 +385,12 @@ SPH_API sph_status sph_server_set_exact(sph_server* sv, int exact)
     return SPH_OK;
 }
 
+// One scheduling round, pipelined with the GPU: it waits for the steps the
+// previous round queued, retires the jobs they finished (their readback is
+// queued into host memory), admits queued jobs (uploads and sorts queued),
+// rebuilds the scene table if it changed and queues this round's steps, then
+// returns while the GPU runs them.  So the host's bookkeeping and the
+// caller's work between rounds overlap the steps.
 SPH_API sph_status sph_server_poll(sph_server* sv, uint32_t chunk_steps, uint32_t* active_out, uint32_t* queued_out)
 {
     if (!sv || chunk_steps == 0) return SPH_ERR_INVALID_ARGUMENT;
@@ -367,6 +402,35 @@ SPH_API sph_status sph_server_poll(sph_server* sv, uint32_t chunk_steps, uint32_
         t = t1;
     };
     ++sv->polls;
+    if (sv->pending) {
+        SRV_CUDA_TRY(cudaEventSynchronize(sv->steps_done));
+        SRV_TRY(sv->arena.check_device_error());   // the round's admissions and steps
+        lap(4);
+        sv->pending = false;
+        std::vector<uint64_t> still;
+        for (size_t k = 0; k < sv->active.size(); ++k) {
+            Job& j = *sv->jobs[sv->active[k]];
+            j.done += sv->pending_steps;
+            if (j.done < j.steps) {
+                still.push_back(j.id);
+                continue;
+            }
+            j.result.resize(j.in.n);
+            if (sv->host_direct) {
+                SRV_TRY(sv->arena.read_scene_async((uint32_t)k, j.result.data()));
+                SRV_CUDA_TRY(cudaEventCreateWithFlags(&j.ready, cudaEventDisableTiming));
+                SRV_CUDA_TRY(cudaEventRecord(j.ready, sv->stream));
+            } else {
+                SRV_TRY(sv->arena.read_scene((uint32_t)k, j.result.data(), nullptr));
+            }
+            j.state = JobState::Finished;
+            release_ranges(sv, j);          // a range reused below is written after the readback
+            sv->finished.push_back(j.id);
+            sv->dirty = true;
+        }
+        sv->active.swap(still);
+        lap(5);
+    }
     // admit in arrival order; later jobs may pass one that does not fit
     for (auto it = sv->queue.begin(); it != sv->queue.end() && sv->active.size() < sv->max_slots;) {
         Job& j = *sv->jobs[*it];
@@ -379,8 +443,6 @@ SPH_API sph_status sph_server_poll(sph_server* sv, uint32_t chunk_steps, uint32_
     }
     lap(0);
     if (!sv->active.empty()) {
-        SRV_TRY(sv->arena.check_device_error());   // the admissions' sorts
-        lap(1);
         if (sv->dirty) {
             std::vector<SceneDesc> descs;
             for (uint64_t id : sv->active) descs.push_back(desc_of(*sv->jobs[id]));
@@ -395,28 +457,11 @@ SPH_API sph_status sph_server_poll(sph_server* sv, uint32_t chunk_steps, uint32_
             steps = std::min(steps, j.steps - j.done);
         }
         SRV_TRY(sv->arena.enqueue_steps(steps, sv->mode, false, false));
+        SRV_CUDA_TRY(cudaEventRecord(sv->steps_done, sv->stream));
+        sv->pending = true;
+        sv->pending_steps = steps;
         sv->steps_run += steps;
         lap(3);
-        SRV_CUDA_TRY(cudaStreamSynchronize(sv->stream));
-        SRV_TRY(sv->arena.check_device_error());
-        lap(4);
-        std::vector<uint64_t> still;
-        for (size_t k = 0; k < sv->active.size(); ++k) {
-            Job& j = *sv->jobs[sv->active[k]];
-            j.done += steps;
-            if (j.done >= j.steps) {
-                j.result.resize(j.in.n);
-                SRV_TRY(sv->arena.read_scene((uint32_t)k, j.result.data(), nullptr));
-                j.state = JobState::Finished;
-                release_ranges(sv, j);
-                sv->finished.push_back(j.id);
-                sv->dirty = true;
-            } else {
-                still.push_back(j.id);
-            }
-        }
-        sv->active.swap(still);
-        lap(5);
     }
     if (active_out) *active_out = (uint32_t)sv->active.size();
     if (queued_out) *queued_out = (uint32_t)sv->queue.size();
@@ -457,6 +502,12 @@ SPH_API sph_status sph_server_result(sph_server* sv, uint64_t job_id, sph_dynami
         return SPH_ERR_NOT_FOUND;
     }
     Job& j = *it->second;
+    if (j.ready) {                       // a readback still in flight
+        SRV_CUDA_TRY(cudaSetDevice(sv->device));
+        SRV_CUDA_TRY(cudaEventSynchronize(j.ready));
+        cudaEventDestroy(j.ready);
+        j.ready = nullptr;
+    }
     if (out) std::copy(j.result.begin(), j.result.end(), out);
     if (density)
         for (uint32_t i = 0; i < j.in.n; ++i) density[i] = j.result[i].pressure / j.gas + j.rho0;

@@ -52,6 +52,29 @@ struct SceneInput {
 
 enum class StepMode { Staged = 0, Persistent = 1 };
 
+// Launch shapes of the two neighbour passes in the default arithmetic
+// (sph_shapes.cu): threads per CTA and the register bound's resident CTAs
+// per SM.  Shape 0 is the default kernel; every shape computes the same
+// bits.
+constexpr int kShapeCount = 5;
+struct ShapeInfo {
+    int threads;
+    int min_ctas;
+};
+constexpr ShapeInfo kShapeInfo[kShapeCount] = {
+    {kTileThreads, SPH_DENSITY_MIN_CTAS}, {64, 14}, {256, 3}, {128, 6}, {128, 8}};
+cudaError_t launch_shaped(int shape, bool density, const StepArgs& a, cudaStream_t s);
+
+// One configuration of the step: staged (with the two passes' shapes) or
+// persistent (with its grid), and its measured time per step.
+struct TuneChoice {
+    StepMode mode;
+    uint32_t ctas;          // persistent grid, 0 = the occupancy limit
+    int density_shape;
+    int force_shape;
+    float ms;
+};
+
 void set_last_error(const std::string& s);
 const char* last_error();
 
@@ -133,7 +156,12 @@ public:
                           uint32_t cap_sbm);
     // Uploads one scene into its ranges (d's offsets) and sorts it alone.
     // With sync = false the work is only queued (check_device_error later).
-    sph_status admit_scene(const SceneDesc& d, const SceneInput& in, bool sync = true);
+    // With host_direct the kernels read the scene's particles from the
+    // caller's (pageable) arrays themselves, which must stay valid until the
+    // work completes (GPUs with pageable memory access only).
+    sph_status admit_scene(const SceneDesc& d, const SceneInput& in, bool sync = true, bool host_direct = false);
+    // Queues a readback of one scene into host memory the GPU writes itself.
+    sph_status read_scene_async(uint32_t scene, sph_dynamic_particle* out);
     // Replaces the set of scenes the step advances (table, tiles, scan range).
     sph_status set_active(const std::vector<SceneDesc>& descs);
     uint32_t cap_n() const { return cap_n_; }
@@ -153,6 +181,25 @@ public:
     sph_status restore_state();
     // Occupancy-limited CTAs per SM of the persistent step kernel.
     sph_status persistent_capacity(uint32_t* sms, uint32_t* per_sm);
+
+    // Launch shapes of the staged step's density and force passes (default
+    // arithmetic, accelerations not recorded); 0 = the default kernels.
+    void set_shapes(int density, int force)
+    {
+        if (density != density_shape_ || force != force_shape_) drop_graphs();
+        density_shape_ = density;
+        force_shape_ = force;
+    }
+    int density_shape() const { return density_shape_; }
+    int force_shape() const { return force_shape_; }
+
+    // The launch autotuner (sph_tune.cu): times the staged step under each
+    // launch shape of the two neighbour passes and, with allow_persistent,
+    // the persistent step at each grid size, on a saved copy of the state
+    // (which replaces any earlier save_state copy); applies and returns the
+    // fastest.  Choices are cached per GPU and size class.
+    sph_status autotune(uint32_t trial_steps, bool allow_persistent, TuneChoice* out, bool* from_cache);
+    void apply_choice(const TuneChoice& c);
 
     const float* stage_ms() const { return stage_ms_; }
     void set_persistent_ctas(uint32_t c)
@@ -218,6 +265,7 @@ private:
     sph_status launch_step_staged(bool record_accel, bool timed);
     unsigned overflow_grid(unsigned tiles_n);
     StepArgs step_args() const;
+    std::string tune_key(bool allow_persistent) const;
 
     int device_ = 0;
     cudaStream_t stream_ = nullptr;
@@ -231,6 +279,7 @@ private:
     cudaEvent_t events_[6] = {};
     float stage_ms_[5] = {};
     uint32_t persistent_ctas_ = 0;
+    int density_shape_ = 0, force_shape_ = 0;
     bool exact_ = false;
     uint32_t sm_count_ = 0;
     uint32_t grid_cache_ = 0;
@@ -238,6 +287,7 @@ private:
              max_tiles_ = 0;
     std::vector<uint32_t> tile_first_;     // first tile of each scene
     Tile* d_tmp_tiles_ = nullptr;          // tiles of a scene being admitted
+    uint32_t* d_tile_first_ = nullptr;     // arena: first tile of each active scene (+ the total)
     float4* saved_pos_ = nullptr;          // save_state() copies
     float4* saved_vel_ = nullptr;
     uint32_t* saved_start_ = nullptr;

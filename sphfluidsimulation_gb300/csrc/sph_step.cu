@@ -50,26 +50,6 @@ __global__ void __launch_bounds__(kTileThreads) k_gather(SortArgs a)
     }
 }
 
-__device__ __forceinline__ NbrArgs nbr_args(const StepArgs& a)
-{
-    return NbrArgs{a.nbr, a.snbr, a.ncount, a.tile_overflow, a.nbr_stride, a.nonfinite};
-}
-
-__device__ __forceinline__ StaticTables static_tables(const StepArgs& a)
-{
-    return StaticTables{a.spos, a.sstart, a.spos_ref, a.sstart_ref, a.sbitmap};
-}
-
-__device__ __forceinline__ TriangleMesh triangle_mesh(const StepArgs& a)
-{
-    return TriangleMesh{a.tris, a.tri_cells, a.tri_list};
-}
-
-__device__ __forceinline__ ForceOut force_out(const StepArgs& a)
-{
-    return ForceOut{a.pos_tmp, a.vel_tmp, a.key, a.arrival, a.count, a.accel, a.nonfinite + 1};
-}
-
 template <bool kExact>
 __global__ void __launch_bounds__(kDensityThreads, SPH_DENSITY_MIN_CTAS) k_density(StepArgs a)
 {
@@ -218,7 +198,7 @@ __global__ void __launch_bounds__(kTileThreads) k_static_bitmap(const Tile* tile
 __global__ void __launch_bounds__(kTileThreads) k_unsort(const Tile* tiles, const SceneDesc* scenes, const float4* pos,
                                                          const float4* vel, float4* out, const float4* accel_in,
                                                          float4* accel_out, const uint32_t* tag_in, uint32_t* tag_out,
-                                                         int by_tag, uint32_t* rank_out = nullptr)
+                                                         int by_tag, uint32_t* rank_out = nullptr, uint32_t out_origin = 0)
 {
     const Tile tile = tiles[blockIdx.x];
     const SceneDesc& sc = scenes[tile.scene];
@@ -233,8 +213,8 @@ __global__ void __launch_bounds__(kTileThreads) k_unsort(const Tile* tiles, cons
     if (!out) return;   // tags only
     const float4 v = vel[i];
     const uint32_t key = fast_mod(cell_hash(p.x, p.y, p.z, sc.h), sc.fm_b);
-    out[2 * (size_t)o] = make_float4(p.x, p.y, p.z, v.w);
-    out[2 * (size_t)o + 1] = make_float4(v.x, v.y, v.z, __uint_as_float(key));
+    out[2 * (size_t)(o - out_origin)] = make_float4(p.x, p.y, p.z, v.w);
+    out[2 * (size_t)(o - out_origin) + 1] = make_float4(v.x, v.y, v.z, __uint_as_float(key));
     if (accel_in) accel_out[o] = accel_in[i];
 }
 
@@ -257,6 +237,50 @@ __global__ void __launch_bounds__(kTileThreads) k_load(const Tile* tiles, const 
     const uint32_t w = statics ? cell_hash(p.x, p.y, p.z, sc.h) : i - sc.p_off;
     pos_tmp[i] = make_float4(p.x, p.y, p.z, __uint_as_float(w));
     vel_tmp[i] = make_float4(v.x, v.y, v.z, statics ? 0.f : p.w);
+}
+
+// The same load straight from the caller's arrays: positions (and
+// velocities, or none) as 3 floats per particle in the caller's order,
+// element k of the view at slot p_off + k.  Used where the GPU reads
+// pageable host memory directly (Grace's address translation on GB300), so
+// a job's particles need neither a host repack nor a staging copy.
+__global__ void __launch_bounds__(kTileThreads) k_load_points(const Tile* tiles, const SceneDesc* scenes,
+                                                              const float* p3, const float* v3, float4* pos_tmp,
+                                                              float4* vel_tmp, int statics)
+{
+    const Tile tile = tiles[blockIdx.x];
+    const SceneDesc& sc = scenes[tile.scene];
+    const uint32_t i = tile.begin + threadIdx.x;
+    if (i >= tile.end) return;
+    const size_t k = i - sc.p_off;
+    const float x = p3[3 * k], y = p3[3 * k + 1], z = p3[3 * k + 2];
+    float vx = 0.f, vy = 0.f, vz = 0.f;
+    if (v3) {
+        vx = v3[3 * k];
+        vy = v3[3 * k + 1];
+        vz = v3[3 * k + 2];
+    }
+    const uint32_t w = statics ? cell_hash(x, y, z, sc.h) : (uint32_t)k;
+    pos_tmp[i] = make_float4(x, y, z, __uint_as_float(w));
+    vel_tmp[i] = make_float4(vx, vy, vz, 0.f);
+}
+
+// The tile table of a scene table, built on the device: tile t belongs to
+// the scene k with first[k] <= t < first[k + 1] (first[n_scenes] = total)
+// and covers kTileThreads slots of it.
+__global__ void __launch_bounds__(kTileThreads) k_build_tiles(const SceneDesc* scenes, const uint32_t* first,
+                                                              uint32_t n_scenes, Tile* out, uint32_t total)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    uint32_t lo = 0, hi = n_scenes;          // the last scene whose first tile is <= t
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (first[mid] <= t) lo = mid; else hi = mid;
+    }
+    const SceneDesc& d = scenes[lo];
+    const uint32_t b = (t - first[lo]) * (uint32_t)kTileThreads;
+    out[t] = Tile{lo, d.p_off + b, d.p_off + min(b + (uint32_t)kTileThreads, d.n), 0u};
 }
 
 // ---------------------------------------------------------------------------
@@ -338,7 +362,7 @@ void StepState::free_device_arrays()
                     sstart_ref, tris,
                     accel, accel_tmp, accel_io, staging, d_tmp_tiles_, d_tmp_scene_, nbr, snbr, ncount, tile_overflow,
                     saved_pos_, saved_vel_, saved_start_, sbitmap, tag, tag_io, rank_io, saved_tag_, tri_cells, tri_list,
-                    render_zkey_, render_rgba_, render_depth_};
+                    render_zkey_, render_rgba_, render_depth_, d_tile_first_};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     d_scenes = d_sscenes = d_sfscenes = d_tmp_scene_ = nullptr;
@@ -355,6 +379,7 @@ void StepState::free_device_arrays()
     spos_ref = nullptr;
     sstart_ref = nbr = snbr = ncount = tile_overflow = sbitmap = nullptr;
     d_tiles = d_stiles = d_tmp_tiles_ = nullptr;
+    d_tile_first_ = nullptr;
     pos = vel = pos_tmp = vel_tmp = spos = accel = accel_tmp = accel_io = nullptr;
     staging = nullptr;
     key = arrival = ptag = count = start = scan_ticket = err = bar = nonfinite = sstart = nullptr;
@@ -546,6 +571,7 @@ sph_status StepState::alloc_arrays(uint32_t cap_n, uint32_t cap_q, uint32_t cap_
     ALLOC(d_stiles, max_tiles_);
     ALLOC(d_tmp_tiles_, tiles_for(work_n) + 1);
     ALLOC(d_tmp_scene_, 3);
+    ALLOC(d_tile_first_, max_scenes_ + 1);
     ALLOC(pos, cap_n);
     ALLOC(vel, cap_n);
     ALLOC(pos_tmp, work_n);
@@ -812,7 +838,7 @@ sph_status StepState::grow_arena(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s,
 // Sorts one scene alone: its own tiles and one-entry scene tables, and scans
 // over its own bucket ranges only, so every other scene's table is untouched
 // (a sub-range scan yields local starts; the per-scene delta absorbs that).
-sph_status StepState::admit_scene(const SceneDesc& d, const SceneInput& in, bool sync)
+sph_status StepState::admit_scene(const SceneDesc& d, const SceneInput& in, bool sync, bool host_direct)
 {
     if (d.p_off + (uint64_t)d.n > cap_n_ || d.q_off + (uint64_t)d.buckets > cap_q_ ||
         d.s_off + (uint64_t)d.s > cap_s_ || d.sq_off + (uint64_t)d.s > cap_sq_ ||
@@ -839,13 +865,20 @@ sph_status StepState::admit_scene(const SceneDesc& d, const SceneInput& in, bool
         CUDA_TRY(cudaMemcpyAsync(d_tmp_tiles_, tl.data(), sizeof(Tile) * tl.size(), cudaMemcpyHostToDevice, stream_));
         const unsigned nt = (unsigned)tl.size();
         if (kind != 2) {   // the second static sort reuses the first one's loaded particles
-            if (kind == 1) {
-                if ((st = upload_particles(stream_, staging, v.p_off, in.spos, nullptr, v.n)) != SPH_OK) return st;
+            if (host_direct) {
+                k_load_points<<<nt, kTileThreads, 0, stream_>>>(d_tmp_tiles_, d_tmp_scene_,
+                                                                kind == 1 ? in.spos : in.pos,
+                                                                kind == 1 ? nullptr : in.vel, pos_tmp, vel_tmp,
+                                                                kind != 0 ? 1 : 0);
             } else {
-                if ((st = upload_particles(stream_, staging, v.p_off, in.pos, in.vel, v.n)) != SPH_OK) return st;
+                if (kind == 1) {
+                    if ((st = upload_particles(stream_, staging, v.p_off, in.spos, nullptr, v.n)) != SPH_OK) return st;
+                } else {
+                    if ((st = upload_particles(stream_, staging, v.p_off, in.pos, in.vel, v.n)) != SPH_OK) return st;
+                }
+                k_load<<<nt, kTileThreads, 0, stream_>>>(d_tmp_tiles_, d_tmp_scene_, staging, pos_tmp, vel_tmp,
+                                                         kind != 0 ? 1 : 0);
             }
-            k_load<<<nt, kTileThreads, 0, stream_>>>(d_tmp_tiles_, d_tmp_scene_, staging, pos_tmp, vel_tmp,
-                                                     kind != 0 ? 1 : 0);
             CUDA_TRY(cudaGetLastError());
         }
         SortArgs a = sort_args(kind);
@@ -875,28 +908,37 @@ sph_status StepState::set_active(const std::vector<SceneDesc>& descs)
     }
     drop_graphs();
     scenes = descs;
-    tiles.clear();
     tile_first_.clear();
-    uint64_t qmax = 0, tn = 0;
+    uint64_t qmax = 0, tn = 0, nt = 0;
     for (size_t k = 0; k < scenes.size(); ++k) {
         const SceneDesc& d = scenes[k];
-        tile_first_.push_back((uint32_t)tiles.size());
-        for (uint32_t b = 0; b < d.n; b += kTileThreads)
-            tiles.push_back(Tile{(uint32_t)k, d.p_off + b, d.p_off + std::min<uint32_t>(b + kTileThreads, d.n), 0});
+        tile_first_.push_back((uint32_t)nt);
+        nt += (d.n + kTileThreads - 1) / kTileThreads;
         qmax = std::max<uint64_t>(qmax, (uint64_t)d.q_off + d.buckets);
         tn += d.n;
     }
-    if (tiles.size() > max_tiles_) {
+    if (nt > max_tiles_) {
         set_last_error("tile table overflow");
         return SPH_ERR_CAPACITY;
     }
+    // the host keeps only the count; the table itself is built on the device
+    tiles.resize(nt);
     total_n = (uint32_t)tn;
     scan_len = (uint32_t)qmax + 1u;
-    if (!scenes.empty())
+    if (!scenes.empty()) {
+        std::vector<uint32_t> first(tile_first_);
+        first.push_back((uint32_t)nt);
+        // copies from pageable memory are staged when the call returns, so
+        // the host tables may change right away; stream order does the rest
         CUDA_TRY(cudaMemcpyAsync(d_scenes, scenes.data(), sizeof(SceneDesc) * scenes.size(), cudaMemcpyHostToDevice, stream_));
-    if (!tiles.empty())
-        CUDA_TRY(cudaMemcpyAsync(d_tiles, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice, stream_));
-    CUDA_TRY(cudaStreamSynchronize(stream_));
+        CUDA_TRY(cudaMemcpyAsync(d_tile_first_, first.data(), sizeof(uint32_t) * first.size(), cudaMemcpyHostToDevice,
+                                 stream_));
+        if (nt) {
+            k_build_tiles<<<(unsigned)((nt + kTileThreads - 1) / kTileThreads), kTileThreads, 0, stream_>>>(
+                d_scenes, d_tile_first_, (uint32_t)scenes.size(), d_tiles, (uint32_t)nt);
+            CUDA_TRY(cudaGetLastError());
+        }
+    }
     return SPH_OK;
 }
 
@@ -1041,14 +1083,20 @@ sph_status StepState::launch_step_staged(bool record_accel, bool timed)
         s.accel_dst = accel;
     }
     if (timed) CUDA_TRY(cudaEventRecordWithFlags(events_[0], stream_, cudaEventRecordExternal));
-    k_density<kExact><<<nt, kDensityThreads, 0, stream_>>>(a);
+    if (!kExact && density_shape_ > 0)
+        CUDA_TRY(launch_shaped(density_shape_, true, a, stream_));
+    else
+        k_density<kExact><<<nt, kDensityThreads, 0, stream_>>>(a);
     CUDA_TRY(cudaGetLastError());
     if (timed) CUDA_TRY(cudaEventRecordWithFlags(events_[1], stream_, cudaEventRecordExternal));
     if (record_accel) {
         k_force<true, kExact><<<nt, kTileThreads, 0, stream_>>>(a);
         k_force_overflow<true, kExact><<<overflow_grid(nt), kTileThreads, 0, stream_>>>(a);
     } else {
-        k_force<false, kExact><<<nt, kTileThreads, 0, stream_>>>(a);
+        if (!kExact && force_shape_ > 0)
+            CUDA_TRY(launch_shaped(force_shape_, false, a, stream_));
+        else
+            k_force<false, kExact><<<nt, kTileThreads, 0, stream_>>>(a);
         k_force_overflow<false, kExact><<<overflow_grid(nt), kTileThreads, 0, stream_>>>(a);
     }
     CUDA_TRY(cudaGetLastError());
@@ -1271,6 +1319,24 @@ sph_status StepState::read_scene(uint32_t scene, sph_dynamic_particle* out, floa
         }
     }
     return check_device_error();
+}
+
+// Queues the readback of one scene in the caller's order straight into host
+// memory the GPU can write (pageable memory on a GPU with pageable memory
+// access): no staging copy, no wait.  `out` must stay valid until the work
+// completes.
+sph_status StepState::read_scene_async(uint32_t scene, sph_dynamic_particle* out)
+{
+    if (scene >= scenes.size()) return SPH_ERR_NOT_FOUND;
+    const SceneDesc& d = scenes[scene];
+    if (!d.n) return SPH_OK;
+    const uint32_t t0 = tile_first_[scene];
+    const uint32_t t1 = scene + 1 < tile_first_.size() ? tile_first_[scene + 1] : (uint32_t)tiles.size();
+    if (t1 > t0)
+        k_unsort<<<t1 - t0, kTileThreads, 0, stream_>>>(d_tiles + t0, d_scenes, pos, vel, reinterpret_cast<float4*>(out),
+                                                        nullptr, nullptr, tag, nullptr, 0, nullptr, d.p_off);
+    CUDA_TRY(cudaGetLastError());
+    return SPH_OK;
 }
 
 // Replaces one scene's particles from host (caller's order) and re-sorts the

@@ -192,6 +192,17 @@ class SimulationEngineCUDA:
         check(self.lib.sph_engine_read_acceleration(self.h, _fptr(out)), "sph_engine_read_acceleration")
         return out
 
+    def autotune(self, trial_steps: int = 3) -> dict:
+        """Launch shapes of the density and force passes chosen by timing
+        (sph_engine_autotune); replaces a save_state() copy."""
+        cfg = _lib.SphLaunchConfig()
+        check(self.lib.sph_engine_autotune(self.h, int(trial_steps), C.byref(cfg)), "sph_engine_autotune")
+        return {name: getattr(cfg, name) for name, _ in cfg._fields_}
+
+    def set_launch_shapes(self, density_shape: int, force_shape: int) -> None:
+        check(self.lib.sph_engine_set_launch_shapes(self.h, int(density_shape), int(force_shape)),
+              "sph_engine_set_launch_shapes")
+
     def save_state(self) -> None:
         """Device-side checkpoint (sph_engine_save_state)."""
         check(self.lib.sph_engine_save_state(self.h), "sph_engine_save_state")
@@ -292,6 +303,12 @@ class Batch:
         check(self.lib.sph_batch_autotune(self.h, int(trial_steps), C.byref(mode), C.byref(grid), C.byref(ms)),
               "sph_batch_autotune")
         return mode.value, grid.value, ms.value
+
+    def launch_config(self) -> dict:
+        """The step configuration in use (sph_batch_launch_config)."""
+        cfg = _lib.SphLaunchConfig()
+        check(self.lib.sph_batch_launch_config(self.h, C.byref(cfg)), "sph_batch_launch_config")
+        return {name: getattr(cfg, name) for name, _ in cfg._fields_}
 
     def read_scene(self, scene_id: int) -> np.ndarray:
         out = np.zeros(self.sizes[scene_id], DYN_DTYPE)

@@ -477,3 +477,31 @@ def test_fp32_issue_probe():
           f"({rate.value / (props.multi_processor_count * 4):.4e} per scheduler per s)")
     assert ms.value >= 50.0
     assert 0.2 * ceiling < rate.value <= ceiling
+
+
+def test_launch_shapes_compute_the_same_bits():
+    """Every launch shape of the two neighbour passes (threads per CTA x
+    register bound) gives the default shape's bytes, and the autotuner's
+    choice (staged step of one engine) as well."""
+    sc = small_scene()
+    ref = SimulationEngineCUDA()
+    ref.initialize(sc)
+    ref.update(sc.dt, 12)
+    want = ref.read_dynamic_buffer().tobytes()
+    for d, f in [(1, 1), (2, 2), (3, 3), (4, 4), (2, 1), (1, 4)]:
+        e = SimulationEngineCUDA()
+        e.initialize(sc)
+        e.set_launch_shapes(d, f)
+        e.update(sc.dt, 12)
+        assert e.read_dynamic_buffer().tobytes() == want, (d, f)
+    e = SimulationEngineCUDA()
+    e.initialize(sc)
+    cfg = e.autotune(2)
+    assert cfg["mode"] == 1 and cfg["density_threads"] in (64, 128, 256) and cfg["ms_per_step"] > 0
+    again = SimulationEngineCUDA()
+    again.initialize(sc)
+    assert again.autotune(2)["from_cache"] == 1          # same GPU and size class
+    e.update(sc.dt, 12)
+    assert e.read_dynamic_buffer().tobytes() == want
+    with pytest.raises(SphError):
+        e.set_launch_shapes(5, 0)

@@ -170,3 +170,24 @@ def test_finished_reports_each_job_once():
     assert srv.finished() == []
     for jid, sc in zip(ids, scs):
         assert srv.result(jid)[0].tobytes() == alone(sc).tobytes()
+
+
+def test_poll_phases_are_reported():
+    """sph_server_stats: every poll is counted, the steps run add up to the
+    largest horizon served, and the host time of each phase is recorded."""
+    scs = [job(1500, 6, 31), job(800, 11, 32)]
+    srv = Server(budget_bytes=1 << 30, max_slots=4)
+    ids = [srv.submit(sc) for sc in scs]
+    polls = 0
+    while True:
+        a, q = srv.poll(4)
+        polls += 1
+        if a == 0 and q == 0:
+            break
+    st = srv.stats()
+    assert st["polls"] == polls
+    assert st["steps"] == 11
+    assert all(st[k] >= 0.0 for k in st if k.endswith("_s"))
+    assert st["steps_wait_s"] > 0.0
+    for jid, sc in zip(ids, scs):
+        assert srv.result(jid)[0].tobytes() == alone(sc).tobytes()
