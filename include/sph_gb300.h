@@ -189,19 +189,26 @@ SPH_API sph_status sph_engine_set_timing(sph_engine* engine, int on);
 SPH_API sph_status sph_engine_kernel_times(sph_engine* engine, float* ms, int count);
 
 /* Neighbour statistics of the current state, for measurement (one extra
- * launch and a synchronisation; no effect on the simulation).  The density
- * pass tests every dynamic particle of the 27 neighbour buckets it does not
- * skip (SF:397-495 tests all of them): `candidates` counts those tests and
- * `warp_slots` the lane-slots a warp spends on them, since each bucket costs
- * a warp its largest member count.  `neighbours` counts dynamic pairs
- * within h (each ordered pair once), `static_neighbours` static particles
- * within h of a dynamic one. */
+ * launch and a synchronisation; no effect on the simulation).  The per-slot
+ * walk of the density pass (launch shape 5) tests every dynamic particle of
+ * the 27 neighbour buckets it does not skip (SF:397-495 tests all of them):
+ * `candidates` counts those tests and `warp_slots` the lane-slots a warp
+ * spends on them, since each bucket costs a warp its largest member count.
+ * The group walk (the default) tests each slot against every member of its
+ * 27 buckets, 32 candidates per lane-slot round: `group_candidates` counts
+ * those tests and `group_lane_slots` the lane-slots spent (32 per round);
+ * `group_fallback` counts the slots it leaves to the per-slot walk.
+ * `neighbours` counts dynamic pairs within h (each ordered pair once),
+ * `static_neighbours` static particles within h of a dynamic one. */
 typedef struct sph_neighbour_stats {
     uint64_t particles;
     uint64_t candidates;
     uint64_t warp_slots;
     uint64_t neighbours;
     uint64_t static_neighbours;
+    uint64_t group_candidates;
+    uint64_t group_lane_slots;
+    uint64_t group_fallback;
 } sph_neighbour_stats;
 SPH_API sph_status sph_engine_neighbour_stats(sph_engine* engine, sph_neighbour_stats* out);
 
@@ -215,6 +222,7 @@ typedef struct sph_launch_config {
     int force_min_ctas;
     float ms_per_step;         /* measured by the autotuner (or its cache)     */
     int from_cache;            /* 1: taken from the autotuner's cache          */
+    int density_walk;          /* density pass: 0 group walk, 1 per-slot walk  */
 } sph_launch_config;
 
 /* The launch autotuner of sph_batch_autotune for one engine's staged step
@@ -226,7 +234,8 @@ SPH_API sph_status sph_engine_autotune(sph_engine* engine, uint32_t trial_steps,
 /* Sets the launch shapes of the engine's density and force passes by index
  * (0 = 128 x 7, the default; 1 = 64 x 14; 2 = 256 x 3; 3 = 128 x 6; 4 =
  * 128 x 8; threads per CTA x resident CTAs per SM), as the autotuner does.
- * Results do not depend on the shapes. */
+ * Density also has shape 5: 128 x 7 with the per-slot walk in place of the
+ * group walk.  Results do not depend on the shapes. */
 SPH_API sph_status sph_engine_set_launch_shapes(sph_engine* engine, int density_shape, int force_shape);
 
 /* Device-side checkpoint of the scene (one per engine, kept on the device):

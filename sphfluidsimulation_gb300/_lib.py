@@ -41,12 +41,14 @@ class SphRenderLayer(C.Structure):
 class SphLaunchConfig(C.Structure):
     _fields_ = [("mode", C.c_int), ("persistent_ctas", C.c_uint32), ("density_threads", C.c_int),
                 ("density_min_ctas", C.c_int), ("force_threads", C.c_int), ("force_min_ctas", C.c_int),
-                ("ms_per_step", C.c_float), ("from_cache", C.c_int)]
+                ("ms_per_step", C.c_float), ("from_cache", C.c_int), ("density_walk", C.c_int)]
 
 
 class SphNeighbourStats(C.Structure):
     _fields_ = [("particles", C.c_uint64), ("candidates", C.c_uint64), ("warp_slots", C.c_uint64),
-                ("neighbours", C.c_uint64), ("static_neighbours", C.c_uint64)]
+                ("neighbours", C.c_uint64), ("static_neighbours", C.c_uint64),
+                ("group_candidates", C.c_uint64), ("group_lane_slots", C.c_uint64),
+                ("group_fallback", C.c_uint64)]
 
 
 STATUS = {0: "SPH_OK", 1: "SPH_ERR_INVALID_ARGUMENT", 2: "SPH_ERR_NOT_INITIALIZED", 3: "SPH_ERR_CUDA",

@@ -337,13 +337,16 @@ SPH_API sph_status sph_engine_neighbour_stats(sph_engine* e, sph_neighbour_stats
     if (!e || !out) return SPH_ERR_INVALID_ARGUMENT;
     if (!e->initialized) return SPH_ERR_NOT_INITIALIZED;
     API_CUDA_TRY(cudaSetDevice(e->device));
-    uint64_t v[5];
+    uint64_t v[sph::kNeighbourStats];
     API_TRY(e->state.neighbour_stats(v));
     out->particles = v[0];
     out->candidates = v[1];
     out->warp_slots = v[2];
     out->neighbours = v[3];
     out->static_neighbours = v[4];
+    out->group_candidates = v[5];
+    out->group_lane_slots = v[6];
+    out->group_fallback = v[7];
     return SPH_OK;
 }
 
@@ -495,6 +498,7 @@ static void fill_config(const StepState& st, const sph::TuneChoice& c, bool from
     out->force_min_ctas = sph::kShapeInfo[st.force_shape()].min_ctas;
     out->ms_per_step = c.ms;
     out->from_cache = from_cache ? 1 : 0;
+    out->density_walk = sph::kShapeInfo[st.density_shape()].slot_walk;
 }
 
 // The launch autotuner over the batch (StepState::autotune, staged shapes
@@ -533,7 +537,7 @@ SPH_API sph_status sph_batch_launch_config(sph_batch* b, sph_launch_config* out)
 SPH_API sph_status sph_engine_set_launch_shapes(sph_engine* e, int density_shape, int force_shape)
 {
     if (!e || density_shape < 0 || density_shape >= sph::kShapeCount || force_shape < 0 ||
-        force_shape >= sph::kShapeCount)
+        force_shape >= sph::kForceShapeCount)
         return SPH_ERR_INVALID_ARGUMENT;
     API_CUDA_TRY(cudaSetDevice(e->device));
     API_CUDA_TRY(cudaStreamSynchronize(e->stream));

@@ -662,8 +662,8 @@ __device__ __forceinline__ Walk make_walk(const SceneDesc& sc, const float4& p, 
 // when their bucket cannot hold another visited cell's particles.
 // on_cell(members) follows each cell's dynamic bucket with the number of
 // candidates tested there (0 when skipped); every lane of a warp calls it
-// 27 times in the same order.
-template <bool kExact, typename FD, typename FS, typename FC>
+// 27 times in the same order.  kDyn = false walks the static buckets only.
+template <bool kExact, bool kDyn = true, typename FD, typename FS, typename FC>
 __device__ __forceinline__ void walk_neighbours_cells(const SceneDesc& sc, uint32_t i, const float4& p,
                                                       const Walk& w, const float4* __restrict__ pos,
                                                       const uint32_t* __restrict__ start, const StaticTables& st,
@@ -671,7 +671,7 @@ __device__ __forceinline__ void walk_neighbours_cells(const SceneDesc& sc, uint3
 {
     const float h2 = sc.h2;
     const float cull2 = __fmul_rn(h2, 1.0001f);
-    const uint32_t delta = sc.p_off - __ldg(start + sc.q_off);
+    const uint32_t delta = kDyn ? sc.p_off - __ldg(start + sc.q_off) : 0u;
     uint32_t sdelta = 0;
     if (w.near_static)
         sdelta = sc.s_off - (w.ref_walk ? __ldg(st.sstart_ref + sc.sq_off) : __ldg(st.sstart + sc.sf_off));
@@ -686,7 +686,7 @@ __device__ __forceinline__ void walk_neighbours_cells(const SceneDesc& sc, uint3
                 const bool far = bd2 > cull2;
                 const uint32_t hsh = neighbour_hash(w.nb, a, b, c);
                 uint32_t members = 0;
-                if (!(far && w.cull_d)) {
+                if (kDyn && !(far && w.cull_d)) {
                     const uint32_t bk = sc.q_off + fast_mod(hsh, sc.fm_b);
                     const uint32_t beg = max(__ldg(start + bk) + delta, sc.p_off);
                     const uint32_t end = min(__ldg(start + bk + 1) + delta, sc.p_off + sc.n);
@@ -697,7 +697,7 @@ __device__ __forceinline__ void walk_neighbours_cells(const SceneDesc& sc, uint3
                     }
                     members = end > beg ? end - beg : 0u;
                 }
-                on_cell(members);
+                if (kDyn) on_cell(members);
                 if (!w.near_static) continue;
                 if (w.ref_walk) {
                     // SF:454-490: bucket hash % s of the reference's table, every member
@@ -740,6 +740,37 @@ __device__ __forceinline__ float4 static_entry_pos(uint32_t e, const StaticTable
 
 constexpr int kDensityThreads = kTileThreads;   // one home slot per thread
 
+// Sum of (h - r)^3 over the first cnt entries of slot i's neighbour list, in
+// list order.  Four neighbours per round, their loads issued together; the
+// next round's entries load while this round's positions arrive.
+template <bool kExact>
+__device__ __forceinline__ float sum_list(const NbrArgs& nl, uint32_t i, uint32_t cnt, const float4* __restrict__ pos,
+                                          const float4& p, float h)
+{
+    const uint32_t stride = nl.stride;
+    float sum_d = 0.f;
+    const uint32_t* lp = nl.nbr + i;
+    uint32_t m = 0;
+    uint32_t n0 = 0, n1 = 0, n2 = 0, n3 = 0;
+    if (SPH_NBR_BATCH == 4 && m + 4 <= cnt) {
+        n0 = lp[0]; n1 = lp[stride]; n2 = lp[2 * (size_t)stride]; n3 = lp[3 * (size_t)stride];
+    }
+    for (; SPH_NBR_BATCH == 4 && m + 4 <= cnt; m += 4, lp += 4 * (size_t)stride) {
+        const uint32_t j0 = n0, j1 = n1, j2 = n2, j3 = n3;
+        if (m + 8 <= cnt) {
+            const uint32_t* ln = lp + 4 * (size_t)stride;
+            n0 = ln[0]; n1 = ln[stride]; n2 = ln[2 * (size_t)stride]; n3 = ln[3 * (size_t)stride];
+        }
+        const float4 q0 = __ldg(pos + j0), q1 = __ldg(pos + j1), q2 = __ldg(pos + j2), q3 = __ldg(pos + j3);
+        sum_d = __fadd_rn(sum_d, w0_of<kExact>(pair_r2<kExact>(q0, p), h));
+        sum_d = __fadd_rn(sum_d, w0_of<kExact>(pair_r2<kExact>(q1, p), h));
+        sum_d = __fadd_rn(sum_d, w0_of<kExact>(pair_r2<kExact>(q2, p), h));
+        sum_d = __fadd_rn(sum_d, w0_of<kExact>(pair_r2<kExact>(q3, p), h));
+    }
+    for (; m < cnt; ++m, lp += stride) sum_d = __fadd_rn(sum_d, w0_of<kExact>(pair_r2<kExact>(__ldg(pos + *lp), p), h));
+    return sum_d;
+}
+
 // One slot per thread.  (Two home particles per thread sharing candidate
 // loads measured 3x slower on GB300: the extra registers cost more occupancy
 // than the loads saved.)
@@ -771,28 +802,8 @@ __device__ __forceinline__ void density_tile(uint32_t tile_index, const Tile& ti
     float sum_d = 0.f, sum_s = 0.f;
     const bool overflow = cnt > kMaxNbr || scnt > kMaxSNbr;
     if (!overflow) {
-        // four neighbours per round: their loads are issued together
-        const uint32_t* lp = nl.nbr + i;
-        uint32_t m = 0;
-        // the next round's entries load while this round's positions arrive
-        uint32_t n0 = 0, n1 = 0, n2 = 0, n3 = 0;
-        if (SPH_NBR_BATCH == 4 && m + 4 <= cnt) {
-            n0 = lp[0]; n1 = lp[stride]; n2 = lp[2 * (size_t)stride]; n3 = lp[3 * (size_t)stride];
-        }
-        for (; SPH_NBR_BATCH == 4 && m + 4 <= cnt; m += 4, lp += 4 * (size_t)stride) {
-            const uint32_t j0 = n0, j1 = n1, j2 = n2, j3 = n3;
-            if (m + 8 <= cnt) {
-                const uint32_t* ln = lp + 4 * (size_t)stride;
-                n0 = ln[0]; n1 = ln[stride]; n2 = ln[2 * (size_t)stride]; n3 = ln[3 * (size_t)stride];
-            }
-            const float4 q0 = __ldg(pos + j0), q1 = __ldg(pos + j1), q2 = __ldg(pos + j2), q3 = __ldg(pos + j3);
-            sum_d = __fadd_rn(sum_d, w0_of<kExact>(pair_r2<kExact>(q0, p), h));
-            sum_d = __fadd_rn(sum_d, w0_of<kExact>(pair_r2<kExact>(q1, p), h));
-            sum_d = __fadd_rn(sum_d, w0_of<kExact>(pair_r2<kExact>(q2, p), h));
-            sum_d = __fadd_rn(sum_d, w0_of<kExact>(pair_r2<kExact>(q3, p), h));
-        }
-        for (; m < cnt; ++m, lp += stride) sum_d = __fadd_rn(sum_d, w0_of<kExact>(pair_r2<kExact>(__ldg(pos + *lp), p), h));
-        lp = nl.snbr + i;
+        sum_d = sum_list<kExact>(nl, i, cnt, pos, p, h);
+        const uint32_t* lp = nl.snbr + i;
         for (uint32_t k = 0; k < scnt; ++k, lp += stride)
             sum_s = __fadd_rn(sum_s, w0_of<kExact>(pair_r2<kExact>(static_entry_pos(*lp, st), p), h));
     } else {
@@ -803,6 +814,289 @@ __device__ __forceinline__ void density_tile(uint32_t tile_index, const Tile& ti
             [&](uint32_t, const float4&, float r2) { sum_s = __fadd_rn(sum_s, w0_of<kExact>(r2, h)); });
         atomicOr(nl.tile_overflow + tile_index, 1u);   // cleared by the overflow force pass
     }
+    nl.ncount[i] = overflow ? (kOverflow | (kOverflow << 16)) : (cnt | (scnt << 16));
+    // SF:497-498
+    const float rho = __fadd_rn(sc.self_density,
+                                __fmul_rn(__fadd_rn(__fmul_rn(sum_d, sc.mass), __fmul_rn(sum_s, sc.mass)), sc.kc));
+    const float pressure = __fmul_rn(sc.gas, __fsub_rn(rho, sc.rho0));
+    reinterpret_cast<float*>(vel + i)[3] = pressure;
+}
+
+// ---- density: the group walk -------------------------------------------------
+//
+// The same pass, bit for bit, organised around cells instead of slots.  All
+// slots of one cell (one Morton code) have the same 27 neighbour buckets, so
+// their candidates are one sequence: the members of the 27 buckets in the
+// walk's order (x outermost, bucket order inside a bucket).  A warp takes its
+// 32 slots cell by cell ("groups"):
+//   1. lanes 0..26 look up one bucket each and a warp scan places them; the
+//      candidates' slots go to shared memory and their positions to
+//      registers, 32 candidates per register slot;
+//   2. for each home of the group, every lane tests its candidates against
+//      the home and a ballot per register slot records the hits: one test
+//      per candidate and lane, no lane waits at a bucket end;
+//   3. each home's lane decodes its hit bits in candidate order, appending
+//      its neighbour list and summing (h - r)^3 in that order, as
+//      density_tile does.
+// The hits are those of density_tile's test (same r^2 arithmetic, same
+// operands; the cells it skips hold none), so the lists, counts and sums are
+// density_tile's.  Where the 27 buckets may repeat, a repeated bucket is a
+// repeated candidate, as in density_tile, and the home itself is skipped at
+// every place it appears.  Slots whose cell holds more than kGroupSlots * 32
+// candidates, and slots at a non-finite position (whose test passes every
+// candidate, padding included), run density_tile itself; statics are walked
+// per slot.
+constexpr uint32_t kGroupSlots = 8;     // candidate registers per lane: 256 candidates per group
+// Candidate slots one warp holds in shared memory: a warp's groups hold
+// about 27 x (32 + cell occupancy) candidates, about 1080 at 8 slots per
+// cell; past the limit the waiting homes are finished first (step 3).
+constexpr uint32_t kWarpCand = 1280;
+
+struct GroupSmem {
+    uint32_t cand[kWarpCand];           // candidate slots, groups back to back
+    uint32_t hits[32][kGroupSlots];     // per home lane: hit bits of its group's candidates
+};
+
+// Static neighbours of one slot in the walk's order: list entries and sum.
+template <bool kExact>
+__device__ __forceinline__ float density_statics(const SceneDesc& sc, uint32_t i, const float4& p, const Walk& w,
+                                                 const StaticTables& st, const NbrArgs& nl, uint64_t keep,
+                                                 uint32_t& scnt)
+{
+    float sum_s = 0.f;
+    scnt = 0;
+    if (!w.near_static) return sum_s;
+    const uint32_t stride = nl.stride;
+    const float h = sc.h;
+    walk_neighbours_cells<kExact, false>(
+        sc, i, p, w, nullptr, nullptr, st, [](uint32_t, const float4&, float) {},
+        [&](uint32_t e, const float4&, float r2) {
+            if (scnt < kMaxSNbr) store_list(nl.snbr + (size_t)scnt * stride + i, e, keep);
+            ++scnt;
+            sum_s = __fadd_rn(sum_s, w0_of<kExact>(r2, h));
+        },
+        [](uint32_t) {});
+    return sum_s;
+}
+
+// Step 2 for one group whose candidates fill kWords register slots: for each
+// home, one ballot per slot (bit l of word s: candidate 32 s + l is within h).
+template <bool kExact, uint32_t kWords>
+__device__ __forceinline__ void group_ballots(uint32_t group, const float (&qx)[kGroupSlots],
+                                              const float (&qy)[kGroupSlots], const float (&qz)[kGroupSlots],
+                                              const float4& p, float h2, GroupSmem& sm, uint32_t wl)
+{
+    uint32_t hm = group;
+    while (hm) {
+        const int hl = __ffs(hm) - 1;
+        hm &= hm - 1u;
+        const float4 hp = make_float4(__shfl_sync(0xffffffffu, p.x, hl), __shfl_sync(0xffffffffu, p.y, hl),
+                                      __shfl_sync(0xffffffffu, p.z, hl), 0.f);
+        uint32_t b[kGroupSlots];
+#pragma unroll
+        for (uint32_t s = 0; s < kGroupSlots; ++s) {
+            b[s] = 0u;
+            if (s < kWords) {
+                const float r2 = pair_r2<kExact>(make_float4(qx[s], qy[s], qz[s], 0.f), hp);
+                b[s] = __ballot_sync(0xffffffffu, !(r2 > h2));
+            }
+        }
+        if (wl == 0u) {
+            uint4* d = reinterpret_cast<uint4*>(sm.hits[hl]);
+            d[0] = make_uint4(b[0], b[1], b[2], b[3]);
+            if (kWords > 4) d[1] = make_uint4(b[4], b[5], b[6], b[7]);
+        }
+    }
+}
+
+// `lane` = the slot's place in the tile; a warp's 32 lanes share one tile.
+template <bool kExact>
+__device__ __forceinline__ void density_group_tile(uint32_t tile_index, const Tile& tile, uint32_t lane,
+                                                   const SceneDesc* scenes, const float4* __restrict__ pos,
+                                                   float4* __restrict__ vel, const uint32_t* __restrict__ start,
+                                                   const StaticTables& st, const NbrArgs& nl, GroupSmem& sm)
+{
+    constexpr unsigned kFull = 0xffffffffu;
+    const SceneDesc& sc = scenes[tile.scene];
+    const uint32_t i = tile.begin + lane;
+    const bool valid = i < tile.end;
+    if (__ballot_sync(kFull, valid) == 0u) return;
+    const uint32_t wl = lane & 31u;
+    const float h = sc.h, h2 = sc.h2;
+    const float4 p = valid ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool nonfinite_seen = *nl.nonfinite != 0u;
+    uint32_t code, ex[3], ey[3], ez[3];
+    bool elig, dup;
+    {
+        const Neighbourhood nb = neighbourhood(p.x, p.y, p.z, h);
+        elig = valid && finite3(p);
+        dup = nb_span(nb) >= sc.buckets;          // the 27 buckets may repeat
+        code = nb.ex1 + nb.ey1 + nb.ez1;
+        ex[0] = nb.ex0; ex[1] = nb.ex1; ex[2] = nb.ex2;
+        ey[0] = nb.ey0; ey[1] = nb.ey1; ey[2] = nb.ey2;
+        ez[0] = nb.ez0; ez[1] = nb.ez1; ez[2] = nb.ez2;
+    }
+    const uint32_t delta = sc.p_off - __ldg(start + sc.q_off);
+    const uint32_t stride = nl.stride;
+    const uint64_t keep = l2_policy_keep();
+    const int ka = (int)wl / 9, kb = ((int)wl / 3) % 3, kc = (int)wl % 3;   // this lane's neighbour cell
+    uint32_t pending = __ballot_sync(kFull, elig);
+    uint32_t fallback = __ballot_sync(kFull, valid && !elig);
+    uint32_t waiting = 0;       // homes whose hit bits wait in shared memory
+    uint32_t cursor = 0;
+    uint32_t my_base = 0, my_words = 0, my_self = 0;
+    bool my_sdup = false;
+    uint32_t cnt = 0;
+    float sum_d = 0.f;
+
+    // step 3, first half, for this lane's home: its hits in candidate order
+    // appended to its neighbour list.  Its own slot is one known candidate
+    // where the buckets are distinct (my_self), else compared at every hit.
+    // step 3 for this lane's home: its hits in candidate order appended to
+    // its neighbour list and summed, one hit per iteration.  The hit words
+    // sit in registers and shift down as each runs out, so a lane's loop runs
+    // once per hit, not once per word and hit.  The home's own slot is one
+    // known candidate where the buckets are distinct (my_self), else
+    // compared at every hit.
+    auto sum_hits = [&]() {
+        const uint32_t* cw = sm.cand + my_base;
+        const uint4 lo = reinterpret_cast<const uint4*>(sm.hits[wl])[0];
+        const uint4 hi = reinterpret_cast<const uint4*>(sm.hits[wl])[1];
+        uint32_t w0 = lo.x, w1 = lo.y, w2 = lo.z, w3 = lo.w, w4 = hi.x, w5 = hi.y, w6 = hi.z, w7 = hi.w;
+        // words past the group's own hold another group's bits
+        if (my_words < 2) w1 = 0u;
+        if (my_words < 3) w2 = 0u;
+        if (my_words < 4) w3 = 0u;
+        if (my_words < 5) w4 = 0u;
+        if (my_words < 6) w5 = 0u;
+        if (my_words < 7) w6 = 0u;
+        if (my_words < 8) w7 = 0u;
+        const uint32_t self_word = dup ? ~0u : my_self >> 5, m = ~(1u << (my_self & 31u));
+        w0 &= self_word == 0u ? m : ~0u; w1 &= self_word == 1u ? m : ~0u;
+        w2 &= self_word == 2u ? m : ~0u; w3 &= self_word == 3u ? m : ~0u;
+        w4 &= self_word == 4u ? m : ~0u; w5 &= self_word == 5u ? m : ~0u;
+        w6 &= self_word == 6u ? m : ~0u; w7 &= self_word == 7u ? m : ~0u;
+        uint32_t base = 0;
+        for (;;) {
+            while (w0 == 0u) {
+                if ((w1 | w2 | w3 | w4 | w5 | w6 | w7) == 0u) return;
+                w0 = w1; w1 = w2; w2 = w3; w3 = w4; w4 = w5; w5 = w6; w6 = w7; w7 = 0u;
+                base += 32u;
+            }
+            const uint32_t b = (uint32_t)__ffs(w0) - 1u;
+            w0 &= w0 - 1u;
+            const uint32_t j = cw[base + b];
+            if (dup && j == i) continue;
+            if (cnt < kMaxNbr) store_list(nl.nbr + (size_t)cnt * stride + i, j, keep);
+            ++cnt;
+            sum_d = __fadd_rn(sum_d, w0_of<kExact>(pair_r2<kExact>(__ldg(pos + j), p), h));
+        }
+    };
+
+    while (pending) {
+        const int leader = __ffs(pending) - 1;
+        const uint32_t lcode = __shfl_sync(kFull, code, leader);
+        const uint32_t group = __ballot_sync(kFull, elig && code == lcode) & pending;
+        pending &= ~group;
+        // step 1: the group's 27 buckets, one per lane
+        const uint32_t gx0 = __shfl_sync(kFull, ex[0], leader), gx1 = __shfl_sync(kFull, ex[1], leader),
+                       gx2 = __shfl_sync(kFull, ex[2], leader);
+        const uint32_t gy0 = __shfl_sync(kFull, ey[0], leader), gy1 = __shfl_sync(kFull, ey[1], leader),
+                       gy2 = __shfl_sync(kFull, ey[2], leader);
+        const uint32_t gz0 = __shfl_sync(kFull, ez[0], leader), gz1 = __shfl_sync(kFull, ez[1], leader),
+                       gz2 = __shfl_sync(kFull, ez[2], leader);
+        const uint32_t hsh = pick3(ka, gx0, gx1, gx2) + pick3(kb, gy0, gy1, gy2) + pick3(kc, gz0, gz1, gz2);
+        // The reference's static buckets of the 27 cells (hash % s): where
+        // two coincide its static walk visits that bucket twice, and so does
+        // density_statics then (walking the reference's own table).
+        bool sdup = false;
+        if (sc.s) {
+            const uint32_t sb = wl < 27u ? fast_mod(hsh, sc.fm_s) : ~wl;
+            const unsigned peers = __match_any_sync(kFull, sb);       // every lane takes part
+            sdup = __ballot_sync(kFull, wl < 27u && __popc(peers) > 1) != 0u;
+        }
+        uint32_t beg = 0, len = 0;
+        if (wl < 27u) {
+            const uint32_t bk = sc.q_off + fast_mod(hsh, sc.fm_b);
+            beg = max(__ldg(start + bk) + delta, sc.p_off);
+            const uint32_t end = min(__ldg(start + bk + 1) + delta, sc.p_off + sc.n);
+            len = end > beg ? end - beg : 0u;
+        }
+        uint32_t incl = len;
+#pragma unroll
+        for (uint32_t o = 1; o < 32u; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(kFull, incl, o);
+            if (wl >= o) incl += t;
+        }
+        const uint32_t total = __shfl_sync(kFull, incl, 31);
+        if (total > kGroupSlots * 32u) {          // a crowded cell: the per-slot walk
+            fallback |= group;
+            continue;
+        }
+        if (cursor + total > kWarpCand) {        // shared memory full: finish the waiting homes
+            if ((waiting >> wl) & 1u) sum_hits();
+            waiting = 0;
+            cursor = 0;
+            __syncwarp();
+        }
+        uint32_t* cw = sm.cand + cursor;
+        const uint32_t excl = incl - len;
+        for (uint32_t m = 0; m < len; ++m) cw[excl + m] = beg + m;
+        __syncwarp();
+        const uint32_t words = (total + 31u) >> 5;
+        float qx[kGroupSlots], qy[kGroupSlots], qz[kGroupSlots];
+#pragma unroll
+        for (uint32_t s = 0; s < kGroupSlots; ++s) {
+            const uint32_t c = s * 32u + wl;
+            qx[s] = qy[s] = qz[s] = __int_as_float(0x7f800000);   // +inf: never within h of a finite home
+            if (c < total) {
+                const float4 q = __ldg(pos + cw[c]);
+                qx[s] = q.x; qy[s] = q.y; qz[s] = q.z;
+            }
+        }
+        // the home's own slot: its place among the candidates of the centre bucket (k = 13)
+        const uint32_t beg13 = __shfl_sync(kFull, beg, 13), pre13 = __shfl_sync(kFull, excl, 13);
+        // step 2: one ballot per home and register slot (a straight-line
+        // instance per slot count)
+        switch (words) {
+        case 1: group_ballots<kExact, 1>(group, qx, qy, qz, p, h2, sm, wl); break;
+        case 2: group_ballots<kExact, 2>(group, qx, qy, qz, p, h2, sm, wl); break;
+        case 3: group_ballots<kExact, 3>(group, qx, qy, qz, p, h2, sm, wl); break;
+        case 4: group_ballots<kExact, 4>(group, qx, qy, qz, p, h2, sm, wl); break;
+        case 5: group_ballots<kExact, 5>(group, qx, qy, qz, p, h2, sm, wl); break;
+        case 6: group_ballots<kExact, 6>(group, qx, qy, qz, p, h2, sm, wl); break;
+        case 7: group_ballots<kExact, 7>(group, qx, qy, qz, p, h2, sm, wl); break;
+        default: group_ballots<kExact, 8>(group, qx, qy, qz, p, h2, sm, wl); break;
+        }
+        if ((group >> wl) & 1u) {
+            my_base = cursor;
+            my_words = words;
+            my_self = pre13 + (i - beg13);
+            my_sdup = sdup;
+        }
+        waiting |= group;
+        cursor += total;
+        __syncwarp();
+    }
+    if ((waiting >> wl) & 1u) sum_hits();
+    if ((fallback >> wl) & 1u) {
+        density_tile<kExact>(tile_index, tile, lane, scenes, pos, vel, start, st, nl);
+        return;
+    }
+    if (!elig) return;
+    // statics, walked per slot where the cell's neighbourhood holds any (its
+    // bit in the static-presence bitmap); the reference's own table only
+    // where the group's reference buckets repeat
+    uint32_t scnt = 0;
+    float sum_s = 0.f;
+    const uint32_t own = code & sc.sbm_mask;
+    if (sc.s && ((__ldg(st.sbitmap + sc.sbm_off + (own >> 5)) >> (own & 31u)) & 1u)) {
+        Walk w = make_walk<kExact>(sc, p, st.sbitmap, nonfinite_seen);
+        w.ref_walk = my_sdup;
+        sum_s = density_statics<kExact>(sc, i, p, w, st, nl, keep, scnt);
+    }
+    const bool overflow = cnt > kMaxNbr || scnt > kMaxSNbr;
+    if (overflow) atomicOr(nl.tile_overflow + tile_index, 1u);   // cleared by the overflow force pass
     nl.ncount[i] = overflow ? (kOverflow | (kOverflow << 16)) : (cnt | (scnt << 16));
     // SF:497-498
     const float rho = __fadd_rn(sc.self_density,

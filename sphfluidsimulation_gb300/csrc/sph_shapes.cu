@@ -3,11 +3,12 @@
 //
 // The default step launches the density and force passes with one CTA of
 // kTileThreads threads per tile and a register bound of 7 resident CTAs per
-// SM.  Here the same per-slot routines (density_tile, force_tile, default
+// SM.  Here the same routines (density_group_tile, force_tile, default
 // arithmetic) run under other shapes: CTAs of 64 or 256 threads (half a tile,
-// or two tiles) and other register bounds.  Each shape does the same work
-// slot for slot, so results are bit-identical across shapes; only the time
-// differs.  The reference sizes its OpenCL work groups from device queries
+// or two tiles) and other register bounds.  Density shape 5 runs the per-slot
+// walk (density_tile) instead of the group walk.  Each shape does the same
+// work slot for slot, so results are bit-identical across shapes; only the
+// time differs.  The reference sizes its OpenCL work groups from device queries
 // (SimulationEngineGPUKernels.cpp:260-291); this engine measures instead
 // (sph_batch_autotune, sph_engine_autotune).
 #include "sph_state.h"
@@ -24,12 +25,17 @@ __device__ __forceinline__ bool shaped_slot(const StepArgs& a, uint32_t* tile, u
     return *tile < a.num_tiles;
 }
 
-template <int kThreads, int kMinCtas>
+template <int kThreads, int kMinCtas, bool kSlotWalk = false>
 __global__ void __launch_bounds__(kThreads, kMinCtas) k_density_shaped(StepArgs a)
 {
+    __shared__ __align__(16) GroupSmem gsm[kSlotWalk ? 1 : kThreads / 32];
     uint32_t t, lane;
     if (!shaped_slot<kThreads>(a, &t, &lane)) return;        // whole warps
-    density_tile<false>(t, a.tiles[t], lane, a.scenes, a.pos, a.vel, a.start, static_tables(a), nbr_args(a));
+    if (kSlotWalk)
+        density_tile<false>(t, a.tiles[t], lane, a.scenes, a.pos, a.vel, a.start, static_tables(a), nbr_args(a));
+    else
+        density_group_tile<false>(t, a.tiles[t], lane, a.scenes, a.pos, a.vel, a.start, static_tables(a),
+                                  nbr_args(a), gsm[threadIdx.x >> 5]);
 }
 
 template <int kThreads, int kMinCtas>
@@ -41,13 +47,13 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) k_force_shaped(StepArgs a)
                              nbr_args(a), force_out(a), lane);
 }
 
-template <int kThreads, int kMinCtas>
+template <int kThreads, int kMinCtas, bool kSlotWalk = false>
 static cudaError_t launch_pair(bool density, const StepArgs& a, cudaStream_t s)
 {
     const uint32_t slots = a.num_tiles * (uint32_t)kTileThreads;
     const unsigned grid = (slots + kThreads - 1) / kThreads;
     if (density)
-        k_density_shaped<kThreads, kMinCtas><<<grid, kThreads, 0, s>>>(a);
+        k_density_shaped<kThreads, kMinCtas, kSlotWalk><<<grid, kThreads, 0, s>>>(a);
     else
         k_force_shaped<kThreads, kMinCtas><<<grid, kThreads, 0, s>>>(a);
     return cudaGetLastError();
@@ -60,6 +66,8 @@ cudaError_t launch_shaped(int shape, bool density, const StepArgs& a, cudaStream
     case 2: return launch_pair<256, 3>(density, a, s);
     case 3: return launch_pair<128, 6>(density, a, s);
     case 4: return launch_pair<128, 8>(density, a, s);
+    case 5:     // density only: the per-slot walk (density_tile)
+        return density ? launch_pair<kTileThreads, SPH_DENSITY_MIN_CTAS, true>(true, a, s) : cudaErrorInvalidValue;
     default: return cudaErrorInvalidValue;     // shape 0 is the default kernel
     }
 }

@@ -53,16 +53,21 @@ struct SceneInput {
 enum class StepMode { Staged = 0, Persistent = 1 };
 
 // Launch shapes of the two neighbour passes in the default arithmetic
-// (sph_shapes.cu): threads per CTA and the register bound's resident CTAs
-// per SM.  Shape 0 is the default kernel; every shape computes the same
-// bits.
-constexpr int kShapeCount = 5;
+// (sph_shapes.cu): threads per CTA, the register bound's resident CTAs per
+// SM and, for density, the walk (0 the group walk, 1 the per-slot walk).
+// Shape 0 is the default kernel; every shape computes the same bits.  The
+// force pass has the first kForceShapeCount shapes.
+constexpr int kShapeCount = 6;
+constexpr int kNeighbourStats = 8;     // counters of k_neighbour_stats
+constexpr int kForceShapeCount = 5;
 struct ShapeInfo {
     int threads;
     int min_ctas;
+    int slot_walk;
 };
 constexpr ShapeInfo kShapeInfo[kShapeCount] = {
-    {kTileThreads, SPH_DENSITY_MIN_CTAS}, {64, 14}, {256, 3}, {128, 6}, {128, 8}};
+    {kTileThreads, SPH_DENSITY_MIN_CTAS, 0}, {64, 14, 0}, {256, 3, 0}, {128, 6, 0}, {128, 8, 0},
+    {kTileThreads, SPH_DENSITY_MIN_CTAS, 1}};
 cudaError_t launch_shaped(int shape, bool density, const StepArgs& a, cudaStream_t s);
 
 // One configuration of the step: staged (with the two passes' shapes) or
@@ -142,7 +147,7 @@ public:
     sph_status read_buckets(uint32_t scene, uint32_t* bucket_starts, uint32_t* slot_ids);
     // particles, candidates, warp candidate slots, dynamic and static
     // neighbours within h, summed over all scenes (k_neighbour_stats)
-    sph_status neighbour_stats(uint64_t out[5]);
+    sph_status neighbour_stats(uint64_t out[kNeighbourStats]);
     sph_status persistent_grid(uint32_t* grid);
     // Outputs of the initial sort of scene 0 (see sph_cell_sort).
     sph_status read_sort(uint32_t* keys, uint32_t* counts, uint32_t* starts, uint32_t* order);

@@ -53,8 +53,9 @@ __global__ void __launch_bounds__(kTileThreads) k_gather(SortArgs a)
 template <bool kExact>
 __global__ void __launch_bounds__(kDensityThreads, SPH_DENSITY_MIN_CTAS) k_density(StepArgs a)
 {
-    density_tile<kExact>(blockIdx.x, a.tiles[blockIdx.x], threadIdx.x, a.scenes, a.pos, a.vel, a.start,
-                         static_tables(a), nbr_args(a));
+    __shared__ __align__(16) GroupSmem gsm[kDensityThreads / 32];
+    density_group_tile<kExact>(blockIdx.x, a.tiles[blockIdx.x], threadIdx.x, a.scenes, a.pos, a.vel, a.start,
+                               static_tables(a), nbr_args(a), gsm[threadIdx.x >> 5]);
 }
 
 template <bool kRecord, bool kExact>
@@ -85,11 +86,14 @@ __global__ void __launch_bounds__(kTileThreads) k_force_overflow(StepArgs a)
 }
 
 // Neighbour statistics of the current state (a measurement, run outside the
-// step): out[0] particles; out[1] dynamic candidates the density walk tests;
-// out[2] the candidate slots the warps spend on them (a cell costs a warp its
-// largest bucket, so out[2] / out[1] is the divergence overhead); out[3]
-// dynamic neighbours within h (each ordered pair once); out[4] static
-// particles within h of a dynamic one.
+// step): out[0] particles; out[1] dynamic candidates the per-slot density
+// walk tests; out[2] the candidate slots the warps spend on them (a cell
+// costs a warp its largest bucket, so out[2] / out[1] is the divergence
+// overhead); out[3] dynamic neighbours within h (each ordered pair once);
+// out[4] static particles within h of a dynamic one; out[5] candidates the
+// group walk tests its homes against (every member of the 27 buckets);
+// out[6] the lane-slots it spends (32 per register slot and home); out[7]
+// slots it leaves to the per-slot walk (crowded cells, non-finite slots).
 __global__ void __launch_bounds__(kTileThreads) k_neighbour_stats(StepArgs a, unsigned long long* out)
 {
     const Tile& tile = a.tiles[blockIdx.x];
@@ -97,7 +101,7 @@ __global__ void __launch_bounds__(kTileThreads) k_neighbour_stats(StepArgs a, un
     const uint32_t i = tile.begin + threadIdx.x;
     const bool valid = i < tile.end;
     const unsigned mask = __ballot_sync(0xffffffffu, valid);
-    unsigned long long v[5] = {valid ? 1ull : 0ull, 0ull, 0ull, 0ull, 0ull};
+    unsigned long long v[kNeighbourStats] = {valid ? 1ull : 0ull};
     if (valid) {
         const float4 p = a.pos[i];
         const Walk w = make_walk<false>(sc, p, a.sbitmap, a.nonfinite[0] != 0u);
@@ -109,12 +113,27 @@ __global__ void __launch_bounds__(kTileThreads) k_neighbour_stats(StepArgs a, un
                 v[1] += m;
                 v[2] += __reduce_max_sync(mask, m);
             });
+        // the group walk: every member of the 27 buckets (density_group_tile)
+        const uint32_t delta = sc.p_off - __ldg(a.start + sc.q_off);
+        uint32_t total = 0;
+        for (int k = 0; k < 27; ++k) {
+            const uint32_t bk = sc.q_off + fast_mod(neighbour_hash(w.nb, k / 9, (k / 3) % 3, k % 3), sc.fm_b);
+            const uint32_t beg = max(__ldg(a.start + bk) + delta, sc.p_off);
+            const uint32_t end = min(__ldg(a.start + bk + 1) + delta, sc.p_off + sc.n);
+            total += end > beg ? end - beg : 0u;
+        }
+        if (finite3(p) && total <= kGroupSlots * 32u) {
+            v[5] = total;
+            v[6] = 32ull * ((total + 31u) / 32u);
+        } else {
+            v[7] = 1;
+        }
     }
 #pragma unroll
-    for (int k = 0; k < 5; ++k)
+    for (int k = 0; k < kNeighbourStats; ++k)
         for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
     if ((threadIdx.x & 31u) == 0u && mask)
-        for (int k = 0; k < 5; ++k) atomicAdd(out + k, v[k]);
+        for (int k = 0; k < kNeighbourStats; ++k) atomicAdd(out + k, v[k]);
 }
 
 // Bounded grid barrier for the persistent kernel (all CTAs co-resident by
@@ -150,6 +169,7 @@ template <bool kExact>
 __global__ void __launch_bounds__(kTileThreads) k_step_persistent(StepArgs a, uint32_t scan_tiles)
 {
     __shared__ ScanSmem sm;
+    __shared__ __align__(16) GroupSmem gsm[kTileThreads / 32];
     // the previous scan (any launch before this one) is complete: clear its
     // tile status so this step's look-back starts from empty
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < scan_tiles; t += gridDim.x * blockDim.x)
@@ -159,7 +179,8 @@ __global__ void __launch_bounds__(kTileThreads) k_step_persistent(StepArgs a, ui
     const ForceOut fo = force_out(a);
     const TriangleMesh tm = triangle_mesh(a);
     for (uint32_t t = blockIdx.x; t < a.num_tiles; t += gridDim.x)
-        density_tile<kExact>(t, a.tiles[t], threadIdx.x, a.scenes, a.pos, a.vel, a.start, st, nl);
+        density_group_tile<kExact>(t, a.tiles[t], threadIdx.x, a.scenes, a.pos, a.vel, a.start, st, nl,
+                                   gsm[threadIdx.x >> 5]);
     grid_barrier(a.bar_count, a.bar_gen, a.err);
     for (uint32_t t = blockIdx.x; t < a.num_tiles; t += gridDim.x) {
         force_tile<false, kExact>(a.tiles[t], a.scenes, a.pos, a.vel, a.tag, st, tm, nl, fo);
@@ -1391,14 +1412,14 @@ sph_status StepState::read_static(uint32_t scene, sph_static_particle* out, uint
     return SPH_OK;
 }
 
-sph_status StepState::neighbour_stats(uint64_t out[5])
+sph_status StepState::neighbour_stats(uint64_t out[kNeighbourStats])
 {
-    for (int k = 0; k < 5; ++k) out[k] = 0;
+    for (int k = 0; k < kNeighbourStats; ++k) out[k] = 0;
     if (tiles.empty()) return SPH_OK;
     unsigned long long* d = nullptr;
-    sph_status st = dev_alloc(&d, 5);
+    sph_status st = dev_alloc(&d, kNeighbourStats);
     if (st != SPH_OK) return st;
-    unsigned long long h[5] = {};
+    unsigned long long h[kNeighbourStats] = {};
     cudaError_t e = cudaMemsetAsync(d, 0, sizeof h, stream_);
     if (e == cudaSuccess) {
         k_neighbour_stats<<<(unsigned)tiles.size(), kTileThreads, 0, stream_>>>(step_args(), d);
@@ -1411,7 +1432,7 @@ sph_status StepState::neighbour_stats(uint64_t out[5])
         set_last_error(std::string("neighbour statistics: ") + cudaGetErrorString(e));
         return SPH_ERR_CUDA;
     }
-    for (int k = 0; k < 5; ++k) out[k] = h[k];
+    for (int k = 0; k < kNeighbourStats; ++k) out[k] = h[k];
     return check_device_error();
 }
 

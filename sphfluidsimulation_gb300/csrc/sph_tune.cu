@@ -53,7 +53,7 @@ void load_cache_file()
         c.mode = mode == 1 ? StepMode::Persistent : StepMode::Staged;
         c.ctas = ctas;
         if (c.density_shape >= 0 && c.density_shape < kShapeCount && c.force_shape >= 0 &&
-            c.force_shape < kShapeCount)
+            c.force_shape < kForceShapeCount)
             g_tune_cache[key] = c;
     }
     std::fclose(f);
@@ -135,12 +135,13 @@ sph_status StepState::autotune(uint32_t trial_steps, bool allow_persistent, Tune
     TuneChoice best{StepMode::Staged, 0u, 0, 0, 0.f};
     sph_status result = trial(best);
     const int shapes = exact_ ? 1 : kShapeCount;     // the exact passes have one shape
+    const int force_shapes = exact_ ? 1 : kForceShapeCount;
     for (int d = 1; result == SPH_OK && d < shapes; ++d) {
         TuneChoice c{StepMode::Staged, 0u, d, 0, 0.f};
         if ((result = trial(c)) == SPH_OK && c.ms < best.ms) best = c;
     }
     const int best_d = best.density_shape;
-    for (int f = 1; result == SPH_OK && f < shapes; ++f) {
+    for (int f = 1; result == SPH_OK && f < force_shapes; ++f) {
         TuneChoice c{StepMode::Staged, 0u, best_d, f, 0.f};
         if ((result = trial(c)) == SPH_OK && c.ms < best.ms) best = c;
     }

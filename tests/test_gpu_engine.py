@@ -348,6 +348,7 @@ def host_neighbour_stats(pos_sorted, starts, h):
     cull = span < np.uint64(b)
     cull2 = np.float32(hf * hf) * np.float32(1.0001)
     members = np.zeros((n, 27), np.int64)
+    total = np.zeros(n, np.int64)          # the group walk: every member of the 27 buckets
     k = 0
     for a in range(3):
         for bb in range(3):
@@ -358,6 +359,7 @@ def host_neighbour_stats(pos_sorted, starts, h):
                 code = e[0][a] + e[1][bb] + e[2][c]
                 m = cnt[(code % np.uint64(b)).astype(np.int64)]
                 members[:, k] = np.where((bd2 > cull2) & cull, 0, m)
+                total += m
                 k += 1
     warps = members[: n // 32 * 32].reshape(-1, 32, 27).max(1).sum(1) * 32
     tail = members[n // 32 * 32:]
@@ -365,7 +367,11 @@ def host_neighbour_stats(pos_sorted, starts, h):
     tree = cKDTree(p.astype(np.float64))
     nbrs = int(tree.query_pairs(float(hf), output_type="ndarray").shape[0]) * 2
     codes = np.stack([e[0][a] + e[1][bb] + e[2][c] for a in range(3) for bb in range(3) for c in range(3)], 1)
-    return {"candidates": int(members.sum()), "warp_slots": slots, "neighbours": nbrs, "span": span, "codes": codes}
+    grouped = total <= 256
+    return {"candidates": int(members.sum()), "warp_slots": slots, "neighbours": nbrs, "span": span, "codes": codes,
+            "group_candidates": int(total[grouped].sum()),
+            "group_lane_slots": int((32 * ((total[grouped] + 31) // 32)).sum()),
+            "group_fallback": int((~grouped).sum())}
 
 
 def host_static_neighbours(pos_sorted, span, codes, spos_ref, sstart_ref, h):
@@ -408,6 +414,9 @@ def test_neighbour_stats_match_host_count():
     for key in ("candidates", "warp_slots"):
         assert abs(got[key] - ref[key]) <= 1e-3 * ref[key], (key, got[key], ref[key])
     assert got["warp_slots"] >= got["candidates"]
+    for key in ("group_candidates", "group_lane_slots", "group_fallback"):
+        assert got[key] == ref[key], (key, got[key], ref[key])
+    assert got["group_lane_slots"] < 1.2 * got["group_candidates"]
     assert abs(got["neighbours"] - ref["neighbours"]) <= 4 + 1e-5 * ref["neighbours"], (got, ref)
     sp, sst = e.read_static()
     stat = host_static_neighbours(pos, ref["span"], ref["codes"], sp["pos"], sst, sc.params.h)
@@ -488,7 +497,7 @@ def test_launch_shapes_compute_the_same_bits():
     ref.initialize(sc)
     ref.update(sc.dt, 12)
     want = ref.read_dynamic_buffer().tobytes()
-    for d, f in [(1, 1), (2, 2), (3, 3), (4, 4), (2, 1), (1, 4)]:
+    for d, f in [(1, 1), (2, 2), (3, 3), (4, 4), (2, 1), (1, 4), (5, 0), (5, 3)]:
         e = SimulationEngineCUDA()
         e.initialize(sc)
         e.set_launch_shapes(d, f)
@@ -504,4 +513,6 @@ def test_launch_shapes_compute_the_same_bits():
     e.update(sc.dt, 12)
     assert e.read_dynamic_buffer().tobytes() == want
     with pytest.raises(SphError):
-        e.set_launch_shapes(5, 0)
+        e.set_launch_shapes(6, 0)
+    with pytest.raises(SphError):
+        e.set_launch_shapes(0, 5)
