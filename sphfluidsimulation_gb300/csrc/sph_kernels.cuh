@@ -926,6 +926,7 @@ __device__ __forceinline__ void density_group_tile(uint32_t tile_index, const Ti
     const float4 p = valid ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const bool nonfinite_seen = *nl.nonfinite != 0u;
     uint32_t code, ex[3], ey[3], ez[3];
+    bool near_static;
     bool elig, dup;
     {
         const Neighbourhood nb = neighbourhood(p.x, p.y, p.z, h);
@@ -935,7 +936,12 @@ __device__ __forceinline__ void density_group_tile(uint32_t tile_index, const Ti
         ex[0] = nb.ex0; ex[1] = nb.ex1; ex[2] = nb.ex2;
         ey[0] = nb.ey0; ey[1] = nb.ey1; ey[2] = nb.ey2;
         ez[0] = nb.ez0; ez[1] = nb.ez1; ez[2] = nb.ez2;
+        // a static particle lies in the cell's neighbourhood (its bit in the
+        // static-presence bitmap)
+        const uint32_t own = code & sc.sbm_mask;
+        near_static = sc.s && ((__ldg(st.sbitmap + sc.sbm_off + (own >> 5)) >> (own & 31u)) & 1u);
     }
+    const uint32_t near_mask = __ballot_sync(kFull, near_static);
     const uint32_t delta = sc.p_off - __ldg(start + sc.q_off);
     const uint32_t stride = nl.stride;
     const uint64_t keep = l2_policy_keep();
@@ -949,9 +955,6 @@ __device__ __forceinline__ void density_group_tile(uint32_t tile_index, const Ti
     uint32_t cnt = 0;
     float sum_d = 0.f;
 
-    // step 3, first half, for this lane's home: its hits in candidate order
-    // appended to its neighbour list.  Its own slot is one known candidate
-    // where the buckets are distinct (my_self), else compared at every hit.
     // step 3 for this lane's home: its hits in candidate order appended to
     // its neighbour list and summed, one hit per iteration.  The hit words
     // sit in registers and shift down as each runs out, so a lane's loop runs
@@ -1010,7 +1013,7 @@ __device__ __forceinline__ void density_group_tile(uint32_t tile_index, const Ti
         // two coincide its static walk visits that bucket twice, and so does
         // density_statics then (walking the reference's own table).
         bool sdup = false;
-        if (sc.s) {
+        if (group & near_mask) {
             const uint32_t sb = wl < 27u ? fast_mod(hsh, sc.fm_s) : ~wl;
             const unsigned peers = __match_any_sync(kFull, sb);       // every lane takes part
             sdup = __ballot_sync(kFull, wl < 27u && __popc(peers) > 1) != 0u;
@@ -1089,8 +1092,7 @@ __device__ __forceinline__ void density_group_tile(uint32_t tile_index, const Ti
     // where the group's reference buckets repeat
     uint32_t scnt = 0;
     float sum_s = 0.f;
-    const uint32_t own = code & sc.sbm_mask;
-    if (sc.s && ((__ldg(st.sbitmap + sc.sbm_off + (own >> 5)) >> (own & 31u)) & 1u)) {
+    if (near_static) {
         Walk w = make_walk<kExact>(sc, p, st.sbitmap, nonfinite_seen);
         w.ref_walk = my_sdup;
         sum_s = density_statics<kExact>(sc, i, p, w, st, nl, keep, scnt);
