@@ -75,11 +75,27 @@ def alg_bytes(stage: str, n: int, s: int) -> float:
     return per * n + extra
 
 
+def _nvtx(name):
+    """Pushes (name) or pops (None) an NVTX range; a profiler marker only."""
+    import torch
+    try:
+        if name is None:
+            torch.cuda.nvtx.range_pop()
+        else:
+            torch.cuda.nvtx.range_push(name)
+    except Exception:
+        pass
+
+
 def pair_rates(samples, stage_ms, first_step: int):
     """Candidate tests and in-range pairs per particle (means of
     sph_engine_neighbour_stats samples over the stage-timing steps) and the
-    rates they imply: density tests `candidates` pairs against h, force
-    evaluates the in-range ones."""
+    rates they imply.  The default density pass (the group walk) tests each
+    particle against every member of its cell's 27 buckets,
+    `group_candidates`, spending `group_lane_slots` lane-slots (32 per
+    ballot round); the per-slot walk (launch shape 5) would test the
+    `candidates` of the cells it does not skip, spending `warp_slots`.
+    Force evaluates the in-range pairs."""
     if not samples:
         return None
     mean = {k: float(np.mean([s[k] for s in samples])) for k in samples[0]}
@@ -87,12 +103,17 @@ def pair_rates(samples, stage_ms, first_step: int):
     dens_s = float(stage_ms[STAGES.index("density")]) * 1e-3
     force_s = float(stage_ms[STAGES.index("force")]) * 1e-3
     in_range = mean["neighbours"] + mean["static_neighbours"]
+    gc = mean.get("group_candidates", 0.0)
     return {
-        "candidates_per_particle": mean["candidates"] / n,
-        "warp_slots_per_particle": mean["warp_slots"] / n,
+        "group_candidates_per_particle": gc / n,
+        "group_lane_slots_per_particle": mean.get("group_lane_slots", 0.0) / n,
+        "group_lane_slots_per_candidate": mean.get("group_lane_slots", 0.0) / gc if gc else None,
+        "group_fallback_fraction": mean.get("group_fallback", 0.0) / n,
+        "slot_walk_candidates_per_particle": mean["candidates"] / n,
+        "slot_walk_warp_slots_per_particle": mean["warp_slots"] / n,
         "neighbours_per_particle": mean["neighbours"] / n,
         "static_neighbours_per_particle": mean["static_neighbours"] / n,
-        "density_candidate_tests_per_s": mean["candidates"] / dens_s if dens_s > 0 else None,
+        "density_candidate_tests_per_s": gc / dens_s if dens_s > 0 else None,
         "force_pair_evals_per_s": in_range / force_s if force_s > 0 else None,
         "steps_sampled": f"{first_step}..{first_step + len(samples) - 1}, every step (the timed window)",
     }
@@ -251,7 +272,12 @@ def run_plain(args, world, rank, local, pg):
     # warm-up (also builds the step graph), then a device checkpoint: every
     # measurement below replays the same steps W+1..W+K from it, bit for bit
     eng.update(scene.dt, args.warmup)
-    launch = eng.autotune(3)          # launch shapes of the two passes, timed on this state
+    if args.launch_shapes:            # fixed launch shapes (density, force), e.g. 5,0: the per-slot walk
+        d_shape, f_shape = (int(x) for x in args.launch_shapes.split(","))
+        eng.set_launch_shapes(d_shape, f_shape)
+        launch = {"density_shape": d_shape, "force_shape": f_shape, "from": "--launch-shapes"}
+    else:
+        launch = eng.autotune(3)      # launch shapes of the two passes, timed on this state
     eng.save_state()
     issue_peak = fp32_issue_peak(local)
 
@@ -279,15 +305,19 @@ def run_plain(args, world, rank, local, pg):
     value = world * n * args.steps / total_s
 
     # per-stage times over the same steps (events around each stage), and
-    # the neighbour walk's counts at each of them
+    # the neighbour walk's counts at each of them.  The NVTX range
+    # "stage_window" marks these launches for ncu (--nvtx --nvtx-include
+    # "stage_window/"), so profiled counts describe the timed steps too.
     eng.restore_state()
     eng.set_timing(True)
     per_step = []
+    _nvtx("stage_window")
     for k in range(args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()
         eng.update(scene.dt, 1)
         per_step.append(eng.kernel_times().astype(np.float64))
+    _nvtx(None)
     eng.set_timing(False)
     eng.restore_state()
     nstats = []
@@ -452,6 +482,8 @@ def main():
     ap.add_argument("--served-horizon-scale", type=float, default=0.1,
                     help="served sample: factor on every job's horizon")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--launch-shapes", default=None,
+                    help="density,force launch shapes instead of the autotuner's (sph_engine_set_launch_shapes)")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the bounded batched/served samples in the default line")
     args = ap.parse_args()
