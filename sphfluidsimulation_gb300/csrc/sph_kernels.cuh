@@ -525,6 +525,11 @@ constexpr uint32_t kMaxNbr = 96;        // dynamic neighbours listed per particl
 constexpr uint32_t kMaxSNbr = 48;       // static neighbours listed per particle
 constexpr uint32_t kOverflow = 0xFFFFu;
 
+// Row length of the neighbour lists: the slot capacity rounded up to 32, so
+// a row's entries for 32 slots starting at a multiple of 32 fill one
+// 128-byte line.
+__host__ __device__ __forceinline__ uint32_t list_stride(uint32_t cap_n) { return (cap_n + 31u) & ~31u; }
+
 struct NbrArgs {
     uint32_t* nbr;         // [kMaxNbr][stride]
     uint32_t* snbr;        // [kMaxSNbr][stride]
@@ -1307,6 +1312,30 @@ __device__ __forceinline__ uint32_t integrate_particle(const SceneDesc& sc, uint
     return k;
 }
 
+// The neighbour lists are dead once the force pass has read them: the next
+// density pass rewrites every entry a force pass reads.  So each warp drops
+// its rows' lines from L2 without writing them back (PTX discard.global.L2:
+// the line's contents become undefined), which keeps the density pass's list
+// writes out of DRAM while they are still in L2.  Only where the warp's 32
+// slots fill their lines alone: every lane a slot of this tile, the first
+// slot a multiple of 32 (rows start at multiples of 32 entries, list_stride).
+// `rows` / `srows`: this lane's dynamic / static entries read (0 if none).
+__device__ __forceinline__ void discard_read_lists(const Tile& tile, uint32_t i, uint32_t lane, const NbrArgs& nl,
+                                                   uint32_t rows, uint32_t srows)
+{
+    const uint32_t wl = lane & 31u;
+    const uint32_t ws = i - wl;                        // the warp's first slot
+    const bool whole = __ballot_sync(0xffffffffu, i < tile.end) == 0xffffffffu && (ws & 31u) == 0u &&
+                       (nl.stride & 31u) == 0u;
+    const uint32_t dr = __reduce_max_sync(0xffffffffu, rows);
+    const uint32_t sr = __reduce_max_sync(0xffffffffu, srows);
+    if (!whole) return;
+    for (uint32_t k = wl; k < dr; k += 32u)
+        asm volatile("discard.global.L2 [%0], 128;" ::"l"(nl.nbr + (size_t)k * nl.stride + ws) : "memory");
+    for (uint32_t k = wl; k < sr; k += 32u)
+        asm volatile("discard.global.L2 [%0], 128;" ::"l"(nl.snbr + (size_t)k * nl.stride + ws) : "memory");
+}
+
 // Where the force pass writes and counts.
 struct ForceOut {
     float4* pos_out;
@@ -1330,12 +1359,15 @@ __device__ __forceinline__ void force_tile(const Tile& tile, const SceneDesc* sc
     const uint32_t i = tile.begin + lane;
     bool valid = i < tile.end;
     uint32_t g = 0;
+    uint32_t listed = 0, slisted = 0;              // list entries this slot reads
     if (valid) {
         const uint32_t c = nl.ncount[i];
         const uint32_t cd = c & 0xFFFFu, cs = c >> 16;
         if (cd == kOverflow || cs == kOverflow) {
             valid = false;                         // handled by force_overflow_tile
         } else {
+            listed = cd;
+            slisted = cs;
             const float h = sc.h;
             const float4 p = pos[i];
             const float4 v = vel[i];
@@ -1381,6 +1413,7 @@ __device__ __forceinline__ void force_tile(const Tile& tile, const SceneDesc* sc
                                                                     o.key_out, o.accel, o.nonfinite_next);
         }
     }
+    discard_read_lists(tile, i, lane, nl, valid ? listed : 0u, valid ? slisted : 0u);
     const uint32_t r = warp_aggregated_increment(o.count, g, valid);
     if (valid) o.arrival[i] = r;
 }

@@ -613,8 +613,8 @@ sph_status StepState::alloc_arrays(uint32_t cap_n, uint32_t cap_q, uint32_t cap_
     ALLOC(sstart, cap_sf + 1ull);
     ALLOC(spos_ref, cap_s);
     ALLOC(sstart_ref, cap_sq + 1ull);
-    ALLOC(nbr, (size_t)kMaxNbr * cap_n);
-    ALLOC(snbr, (size_t)kMaxSNbr * cap_n);
+    ALLOC(nbr, (size_t)kMaxNbr * list_stride(cap_n));
+    ALLOC(snbr, (size_t)kMaxSNbr * list_stride(cap_n));
     ALLOC(ncount, cap_n);
     ALLOC(tile_overflow, max_tiles_);
     ALLOC(sbitmap, cap_sbm);
@@ -832,8 +832,8 @@ sph_status StepState::grow_arena(uint32_t cap_n, uint32_t cap_q, uint32_t cap_s,
     GROW(sstart, cap_sf_ + 1ull, cap_sf + 1ull, false);
     GROW(spos_ref, cap_s_, cap_s, false);
     GROW(sstart_ref, cap_sq_ + 1ull, cap_sq + 1ull, false);
-    GROW(nbr, 0, (size_t)kMaxNbr * cap_n, false);
-    GROW(snbr, 0, (size_t)kMaxSNbr * cap_n, false);
+    GROW(nbr, 0, (size_t)kMaxNbr * list_stride(cap_n), false);
+    GROW(snbr, 0, (size_t)kMaxSNbr * list_stride(cap_n), false);
     GROW(ncount, 0, cap_n, false);
     GROW(tile_overflow, 0, tiles_for(cap_n) + max_scenes_, true);
     GROW(sbitmap, cap_sbm_, std::max<uint32_t>(cap_sbm, 1), true);
@@ -1075,7 +1075,7 @@ StepArgs StepState::step_args() const
     a.snbr = snbr;
     a.ncount = ncount;
     a.tile_overflow = tile_overflow;
-    a.nbr_stride = cap_n_;
+    a.nbr_stride = list_stride(cap_n_);
     return a;
 }
 
