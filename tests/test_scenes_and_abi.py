@@ -75,3 +75,36 @@ def test_no_device_is_an_error_not_a_crash():
     st = lib.sph_engine_create(C.byref(h), 0)
     assert st != 0
     assert lib.sph_last_error() != b""
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """The Python binding's ctypes structs have the C header's layout: every
+    field at the offset the C compiler gives it, and the same total size
+    (a C program built from include/sph_gb300.h prints them)."""
+    import os
+    pairs = {"sph_params": _lib.SphParams, "sph_render_view": _lib.SphRenderView,
+             "sph_render_layer": _lib.SphRenderLayer, "sph_launch_config": _lib.SphLaunchConfig,
+             "sph_neighbour_stats": _lib.SphNeighbourStats}
+    c_names = {"sph_params": ["particle_mass", "gas_constant", "elasticity", "viscosity", "gravity_x",
+                              "gravity_y", "gravity_z", "rest_density", "max_interaction_distance"]}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "sph_gb300.h"', "int main(void) {"]
+    for cname, cls in pairs.items():
+        fields = c_names.get(cname, [f for f, _ in cls._fields_])
+        lines.append(f'printf("{cname} :sizeof %zu\\n", sizeof({cname}));')
+        for f in fields:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(_lib.PKG), "include")
+    subprocess.run(["gcc", "-std=c11", "-I", inc, str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        name, field, value = line.split()
+        got[(name, field)] = int(value)
+    for cname, cls in pairs.items():
+        assert got[(cname, ":sizeof")] == C.sizeof(cls), cname
+        fields = c_names.get(cname, [f for f, _ in cls._fields_])
+        for cf, (pf, _) in zip(fields, cls._fields_):
+            assert got[(cname, cf)] == getattr(cls, pf).offset, (cname, cf)
