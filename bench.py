@@ -457,6 +457,7 @@ def issue_roofline(stage: str, workload: str, stage_ms: float, probe, sm_mhz: fl
     peak = probe["warp_instructions_per_s"]
     out = {"kernel": stage, "achieved": achieved, "peak": peak, "unit": "warp instructions/s",
            "frac": achieved / peak, "warp_instructions_per_launch": inst,
+           "instructions_window": "ncu mean over steps 6..25 of --steps 20 --warmup 5 (profiles/ncu_traffic.txt)",
            "peak_basis": "measured: FP32 FMA microbenchmark (sph_probe_fp32_issue) in this run",
            "probe_ms": probe["probe_ms"]}
     if sm_mhz:
@@ -468,7 +469,7 @@ def issue_roofline(stage: str, workload: str, stage_ms: float, probe, sm_mhz: fl
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=20)     # steps 6..25: the window of profiles/ncu_traffic.txt
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="dam_break_1m",
