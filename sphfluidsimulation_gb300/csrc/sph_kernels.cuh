@@ -1159,9 +1159,12 @@ __device__ __forceinline__ float3 coincident_direction(const float4& p, const ui
 // reference (the kernels return 0) and are skipped.  kExact follows the
 // reference's operations one for one: dir / r by true division, each
 // product rounded, no fused multiply-adds.
-template <bool kExact>
+// kDefer: a coincident pair adds nothing and sets *coincident instead (the
+// caller then repeats the sums with kDefer = false, in the same order).
+template <bool kExact, bool kDefer = false>
 __device__ __forceinline__ void add_dynamic_pair(PairSums& s, const float4& p, const float4& v, float pi, float h,
-                                                 const float4& q, const float4& u, const uint32_t* tag, uint32_t i)
+                                                 const float4& q, const float4& u, const uint32_t* tag, uint32_t i,
+                                                 bool* coincident = nullptr)
 {
     float dx = __fsub_rn(q.x, p.x), dy = __fsub_rn(q.y, p.y), dz = __fsub_rn(q.z, p.z);
     const float r2 = kExact ? __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz))
@@ -1170,6 +1173,10 @@ __device__ __forceinline__ void add_dynamic_pair(PairSums& s, const float4& p, c
     const float r = root_of<kExact>(r2, rinv);
     if (r >= h) return;          // a NaN distance is kept (SF:126-139)
     if (r2 == 0.f || r == 0.f) {
+        if (kDefer) {
+            *coincident = true;
+            return;
+        }
         const float3 d = coincident_direction<kExact>(p, tag, i);
         dx = d.x; dy = d.y; dz = d.z;
     } else if (kExact) {
@@ -1202,9 +1209,9 @@ __device__ __forceinline__ void add_dynamic_pair(PairSums& s, const float4& p, c
 // One static neighbour: dir |p_i| W1 (SF:600-622).  The reference also sums a
 // static viscosity term and multiplies it by 0 (SF:629): for finite values
 // that adds a signed zero to a force that is never -0, so it is omitted.
-template <bool kExact>
+template <bool kExact, bool kDefer = false>
 __device__ __forceinline__ void add_static_pair(PairSums& s, const float4& p, float api, float h, const float4& q,
-                                                const uint32_t* tag, uint32_t i)
+                                                const uint32_t* tag, uint32_t i, bool* coincident = nullptr)
 {
     float dx = __fsub_rn(q.x, p.x), dy = __fsub_rn(q.y, p.y), dz = __fsub_rn(q.z, p.z);
     const float r2 = kExact ? __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz))
@@ -1213,6 +1220,10 @@ __device__ __forceinline__ void add_static_pair(PairSums& s, const float4& p, fl
     const float r = root_of<kExact>(r2, rinv);
     if (r >= h) return;          // a NaN distance is kept (SF:126-139)
     if (r2 == 0.f || r == 0.f) {
+        if (kDefer) {
+            *coincident = true;
+            return;
+        }
         const float3 d = coincident_direction<kExact>(p, tag, i);
         dx = d.x; dy = d.y; dz = d.z;
     } else if (kExact) {
@@ -1374,41 +1385,55 @@ __device__ __forceinline__ void force_tile(const Tile& tile, const SceneDesc* sc
             const float pi = v.w;
             const float rho = __fadd_rn(__fdiv_rn(pi, sc.gas), sc.rho0);   // SF:541
             const uint32_t stride = nl.stride;
-            PairSums s;
-            s.fp = s.fv = s.fs = make_float3(0.f, 0.f, 0.f);
-            // four neighbours per round: eight position/velocity loads in
-            // flight.  The list entries of round r + 1 are loaded while round
-            // r's neighbours arrive, so a round waits on one load, not two.
-            const uint32_t* lp = nl.nbr + i;
+            // The sums over the lists.  Four neighbours per round: eight
+            // position/velocity loads in flight.  The list entries of round
+            // r + 1 are loaded while round r's neighbours arrive, so a round
+            // waits on one load, not two.
             const uint64_t drop = l2_policy_drop();
-            uint32_t k = 0;
-            uint32_t n0 = 0, n1 = 0, n2 = 0, n3 = 0;
-            if (SPH_NBR_BATCH == 4 && k + 4 <= cd) {
-                n0 = load_list(lp, drop); n1 = load_list(lp + stride, drop);
-                n2 = load_list(lp + 2 * (size_t)stride, drop); n3 = load_list(lp + 3 * (size_t)stride, drop);
-            }
-            for (; SPH_NBR_BATCH == 4 && k + 4 <= cd; k += 4, lp += 4 * (size_t)stride) {
-                const uint32_t j0 = n0, j1 = n1, j2 = n2, j3 = n3;
-                if (k + 8 <= cd) {
-                    const uint32_t* ln = lp + 4 * (size_t)stride;
-                    n0 = load_list(ln, drop); n1 = load_list(ln + stride, drop);
-                    n2 = load_list(ln + 2 * (size_t)stride, drop); n3 = load_list(ln + 3 * (size_t)stride, drop);
-                }
-                const float4 q0 = __ldg(pos + j0), q1 = __ldg(pos + j1), q2 = __ldg(pos + j2), q3 = __ldg(pos + j3);
-                const float4 u0 = __ldg(vel + j0), u1 = __ldg(vel + j1), u2 = __ldg(vel + j2), u3 = __ldg(vel + j3);
-                add_dynamic_pair<kExact>(s, p, v, pi, h, q0, u0, tag, i);
-                add_dynamic_pair<kExact>(s, p, v, pi, h, q1, u1, tag, i);
-                add_dynamic_pair<kExact>(s, p, v, pi, h, q2, u2, tag, i);
-                add_dynamic_pair<kExact>(s, p, v, pi, h, q3, u3, tag, i);
-            }
-            for (; k < cd; ++k, lp += stride) {
-                const uint32_t j = load_list(lp, drop);
-                add_dynamic_pair<kExact>(s, p, v, pi, h, __ldg(pos + j), __ldg(vel + j), tag, i);
-            }
             const float api = fabsf(pi);
-            lp = nl.snbr + i;
-            for (uint32_t k = 0; k < cs; ++k, lp += stride)
-                add_static_pair<kExact>(s, p, api, h, static_entry_pos(load_list(lp, drop), st), tag, i);
+            bool coincident = false;
+            auto sums = [&](auto defer_tag) -> PairSums {
+                constexpr bool kDefer = decltype(defer_tag)::value;
+                PairSums s;
+                s.fp = s.fv = s.fs = make_float3(0.f, 0.f, 0.f);
+                const uint32_t* lp = nl.nbr + i;
+                uint32_t k = 0;
+                uint32_t n0 = 0, n1 = 0, n2 = 0, n3 = 0;
+                if (SPH_NBR_BATCH == 4 && k + 4 <= cd) {
+                    n0 = load_list(lp, drop); n1 = load_list(lp + stride, drop);
+                    n2 = load_list(lp + 2 * (size_t)stride, drop); n3 = load_list(lp + 3 * (size_t)stride, drop);
+                }
+                for (; SPH_NBR_BATCH == 4 && k + 4 <= cd; k += 4, lp += 4 * (size_t)stride) {
+                    const uint32_t j0 = n0, j1 = n1, j2 = n2, j3 = n3;
+                    if (k + 8 <= cd) {
+                        const uint32_t* ln = lp + 4 * (size_t)stride;
+                        n0 = load_list(ln, drop); n1 = load_list(ln + stride, drop);
+                        n2 = load_list(ln + 2 * (size_t)stride, drop); n3 = load_list(ln + 3 * (size_t)stride, drop);
+                    }
+                    const float4 q0 = __ldg(pos + j0), q1 = __ldg(pos + j1), q2 = __ldg(pos + j2), q3 = __ldg(pos + j3);
+                    const float4 u0 = __ldg(vel + j0), u1 = __ldg(vel + j1), u2 = __ldg(vel + j2), u3 = __ldg(vel + j3);
+                    add_dynamic_pair<kExact, kDefer>(s, p, v, pi, h, q0, u0, tag, i, &coincident);
+                    add_dynamic_pair<kExact, kDefer>(s, p, v, pi, h, q1, u1, tag, i, &coincident);
+                    add_dynamic_pair<kExact, kDefer>(s, p, v, pi, h, q2, u2, tag, i, &coincident);
+                    add_dynamic_pair<kExact, kDefer>(s, p, v, pi, h, q3, u3, tag, i, &coincident);
+                }
+                for (; k < cd; ++k, lp += stride) {
+                    const uint32_t j = load_list(lp, drop);
+                    add_dynamic_pair<kExact, kDefer>(s, p, v, pi, h, __ldg(pos + j), __ldg(vel + j), tag, i, &coincident);
+                }
+                lp = nl.snbr + i;
+                for (uint32_t k = 0; k < cs; ++k, lp += stride)
+                    add_static_pair<kExact, kDefer>(s, p, api, h, static_entry_pos(load_list(lp, drop), st), tag, i,
+                                                    &coincident);
+                return s;
+            };
+            // Coincident pairs (r = 0, the reference's random direction) are
+            // rare: the first pass leaves them out, and only a particle that
+            // has one sums again with them, in the same order.  Keeping the
+            // random-direction call out of the common loop made force 6 %
+            // faster (0.160 against 0.171 ms on the 1M dam break).
+            PairSums s = sums(std::integral_constant<bool, true>());
+            if (coincident) s = sums(std::integral_constant<bool, false>());
             g = sc.q_off + integrate_particle<kRecordAccel, kExact>(sc, i, p, v, rho, s, tm, o.pos_out, o.vel_out,
                                                                     o.key_out, o.accel, o.nonfinite_next);
         }
