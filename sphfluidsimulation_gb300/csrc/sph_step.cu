@@ -1086,8 +1086,9 @@ sph_status StepState::ensure_events()
     return SPH_OK;
 }
 
-// One step as six launches (plus the scan's two memsets).  With `timed`,
-// events bracket each stage on the launching stream.
+// One step as six launches (the overflow-force kernel clears the scan's
+// look-back state, so no memset).  With `timed`, events bracket each stage
+// on the launching stream.
 template <bool kExact>
 sph_status StepState::launch_step_staged(bool record_accel, bool timed)
 {
