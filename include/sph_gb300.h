@@ -320,16 +320,17 @@ SPH_API sph_status sph_cell_sort(int device, const float* pos, uint32_t n, float
  * by the caller: pos n x 3 floats, keys n, starts buckets+1 (16-byte
  * aligned), order n; the outputs mean what sph_cell_sort's do.  Work is
  * queued on `stream` (a cudaStream_t, NULL = default stream) and the call
- * returns after it finished.  The sort's scratch is a fixed array inside the
- * library (about 4.2 MiB, held on every GPU that loads the library until the
- * process exits), so the call makes no allocation; n is limited to 262144 and
- * buckets to 524288, larger requests fail with SPH_ERR_CAPACITY.  The first
- * call on a device looks up that array's device address (with the device
- * current), so make it before any stream capture; after a cudaDeviceReset
- * the next call looks it up again, since the array then lives in a new
- * context.  All calls share the array: calls that overlap on the GPU race
- * and must be serialised by the caller.  On any status other than SPH_OK
- * the contents of keys, starts and order are undefined. */
+ * returns after it finished, so it cannot be captured into a CUDA graph: on
+ * a capturing stream it queues nothing and returns SPH_ERR_INVALID_ARGUMENT.
+ * The sort's scratch is a fixed array inside the library (about 4.2 MiB,
+ * held on every GPU that loads the library until the process exits), so the
+ * call makes no allocation; n is limited to 262144 and buckets to 524288,
+ * larger requests fail with SPH_ERR_CAPACITY.  The first call on a device
+ * looks up that array's device address (with the device current); after a
+ * cudaDeviceReset the next call looks it up again, since the array then
+ * lives in a new context.  All calls share the array: calls that overlap on
+ * the GPU race and must be serialised by the caller.  On any status other
+ * than SPH_OK the contents of keys, starts and order are undefined. */
 SPH_API sph_status sph_cell_sort_noalloc(const float* pos, uint32_t n, float h, uint32_t buckets,
                                          uint32_t* keys, uint32_t* starts, uint32_t* order, void* stream);
 

@@ -234,12 +234,18 @@ extern "C" SPH_API sph_status sph_cell_sort_noalloc(const float* pos, uint32_t n
         set_last_error("sph_cell_sort_noalloc: starts must be 16-byte aligned");
         return SPH_ERR_INVALID_ARGUMENT;
     }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    NA_TRY(cudaStreamIsCapturing(s, &capture));
+    if (capture != cudaStreamCaptureStatusNone) {   // the call waits for its status word below
+        set_last_error("sph_cell_sort_noalloc: the call is synchronous and cannot be captured into a CUDA graph");
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
     int device = 0;
     NA_TRY(cudaGetDevice(&device));
     uint32_t* scratch = nullptr;
     sph_status st = scratch_address(device, &scratch);
     if (st != SPH_OK) return st;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     NoAllocArgs a{};
     a.pos = pos;
     a.n = n;

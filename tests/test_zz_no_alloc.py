@@ -12,8 +12,9 @@ scratch left by one call must not leak into the next), the capacity edge
 itself (262,144 particles, 524,288 buckets: 513 scan tiles, every one the
 scratch holds), a bucket of more than 8,192 members (kept in arrival order:
 membership exact, order a permutation), an empty input with null buffers, a
-non-default stream, and a call that leaves the device's free memory and the
-torch allocator untouched.  This file is named to be collected last.
+non-default stream, a call that leaves the device's free memory and the
+torch allocator untouched, and a stream under CUDA graph capture (refused).
+This file is named to be collected last.
 """
 import ctypes as C
 
@@ -161,6 +162,34 @@ def test_noalloc_call_allocates_nothing():
     assert free1 == free0
     assert torch.cuda.memory_allocated(0) == alloc0
     assert torch.cuda.memory_reserved(0) == reserved0
+
+
+def test_noalloc_refuses_a_capturing_stream():
+    """The call waits for its device status word, so on a stream under CUDA
+    graph capture it queues nothing and returns SPH_ERR_INVALID_ARGUMENT; the
+    capture stays valid and replays, and the next plain call works."""
+    import torch
+    rng = np.random.default_rng(5)
+    pos = rng.uniform(0.0, 0.5, size=(1_000, 3)).astype(np.float32)
+    b = _Buffers(pos, 2_000)
+    b.h = 0.01
+    s = torch.cuda.Stream(device=0)
+    x = torch.zeros(4, device="cuda:0")
+    torch.cuda.synchronize()
+    lib = _lib.load()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        st = lib.sph_cell_sort_noalloc(C.c_void_p(b.pos.data_ptr()), b.n, b.h, b.buckets,
+                                       C.c_void_p(b.keys.data_ptr()), C.c_void_p(b.starts.data_ptr()),
+                                       C.c_void_p(b.order.data_ptr()), C.c_void_p(s.cuda_stream))
+        x.add_(1.0)
+    assert st == 1   # SPH_ERR_INVALID_ARGUMENT
+    assert b"captured" in lib.sph_last_error()
+    g.replay()
+    torch.cuda.synchronize()
+    assert x.cpu().tolist() == [1.0] * 4
+    assert np.array_equal(b.results()[1], np.full(2_001, 0xFFFFFFFF, np.uint32))   # nothing queued
+    _compare(pos, 0.01, 2_000)
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch():
